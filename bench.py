@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the point-cloud -> octree build on one GB300.
+
+Workload (default): 10,000,000 points from a 32-component isotropic Gaussian
+mixture (sigma 0.5% of the domain, 2% uniform noise), 64-bit Morton codes at
+21 bits per axis, 8 onesweep passes carrying u32 point indices, unique, Karras
+radix tree + edge count, node offsets, octree make+link.  One step = one full
+build of that cloud.  Metric: Mpoints/s of the full build.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gtc|reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle; the reference itself is Rust + Vulkan and cannot run here) on the
+host cores with all threads.  Under torchrun (N > 1) every rank builds its
+own cloud (replicas, weak scaling) and rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "glsl-tree-construction_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mpoints/s full octree build"
+UNIT = "Mpoints/s"
+N_POINTS = 10_000_000
+KEY_BITS = 64
+WORKLOAD = "octree_clustered_10M_u64"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gtc", "reference"], default="gtc")
+    ap.add_argument("--n", type=int, default=N_POINTS, help="points (default: the 10M workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_hbm_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------- clocks -----
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------ algorithmic bytes --
+def algorithmic_bytes(n, u, m, o, K=8):
+    """Compulsory bytes of each stage reading its inputs once and writing its
+    outputs once (per-stage figures of the reference's stage surface)."""
+    P = 8 if K == 8 else 4
+    return {
+        "morton": 16 * n + (K + 4) * n,
+        "histogram": K * n,
+        "onesweep": P * 2 * (K + 4) * n,
+        "unique": (K + 4) * n + (K + 4) * u,
+        "radix_tree": K * u + 11 * m,
+        "edge_count": 10 * m,
+        "prefix_sum": 8 * m,
+        "octree_make": (17 + K) * m + 64 * o,
+        "octree_link": (23 + K) * m + 8 * u,
+    }
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------ reference ---
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle
+    from gtc import workloads as W
+
+    oracle.build()
+    threads = cpu_threads()
+    pts = W.config2_points(args.n, seed=0)
+    # Size the per-step sample so the whole run stays within ~2.5 minutes.
+    t0 = time.perf_counter()
+    oracle.build_octree(pts, KEY_BITS, threads=threads)
+    t_full = time.perf_counter() - t0
+    total_steps = args.steps + max(args.warmup - 1, 0)
+    frac = min(1.0, 150.0 / max(total_steps * t_full, 1e-9))
+    ns = max(1, int(args.n * frac))
+    sample = np.ascontiguousarray(pts[:ns])
+    for _ in range(max(args.warmup - 1, 0)):
+        oracle.build_octree(sample, KEY_BITS, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.build_octree(sample, KEY_BITS, threads=threads)
+    el = time.perf_counter() - t0
+    value = ns * args.steps / el / 1e6
+    desc = (f"first {ns} of the {args.n}-point clustered cloud per step" if ns < args.n
+            else f"the full {args.n}-point clustered cloud per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": args.n, "key_bits": KEY_BITS, "sample_points": ns},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- gtc ----
+def run_gtc(args):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import gtc
+    from gtc import workloads as W
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+
+    n = args.n
+    pts_np = W.config2_points(n, seed=rank)
+    pts = torch.from_numpy(pts_np).to(dev)
+    ctx = gtc.Context(local)
+    plan = gtc.OctreePlan(ctx, n, KEY_BITS, nodes_capacity=n + (n >> 1))
+    for _ in range(max(args.warmup, 3)):
+        plan.launch(pts)
+    torch.cuda.synchronize()
+    ctx.device_status()
+    u, m, o = plan.counts_host()
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    # --- timed region: K full builds on the current stream, per-stage events on
+    stream = torch.cuda.current_stream()
+    ctx.set_profiling(True)
+    ctx.stage_times(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.launch(pts)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    elapsed_ms = e0.elapsed_time(e1)
+    stages = ctx.stage_times(reset=True)
+    ctx.set_profiling(False)
+    ctx.device_status()
+    clocks = clk.summary()
+    if pg:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+
+    # --- the same builds replayed from one CUDA graph (no per-stage events)
+    plan.capture(pts)
+    for _ in range(3):
+        plan.replay()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        plan.replay()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / args.steps
+
+    # --- end to end through the host-buffer entry point (pinned host memory)
+    L = ctx.L
+    hp = ctypes.c_void_p()
+    hn = ctypes.c_void_p()
+    ctx.check(L.gtc_host_alloc(ctypes.byref(hp), n * 16))
+    cap = o + 1024
+    ctx.check(L.gtc_host_alloc(ctypes.byref(hn), cap * 64))
+    ctypes.memmove(hp, pts_np.ctypes.data, n * 16)
+    counts = np.zeros(3, np.uint32)
+    cp = counts.ctypes.data_as(ctypes.c_void_p)
+    for _ in range(2):
+        ctx.check(L.gtc_build_octree_host(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, hn, cap, cp))
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.check(L.gtc_build_octree_host(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, hn, cap, cp))
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    L.gtc_host_free(hp)
+    L.gtc_host_free(hn)
+    assert tuple(int(c) for c in counts) == (u, m, o)
+
+    if rank != 0:
+        return
+
+    # --- roofline of the dominant kernel (onesweep digit-binning pass)
+    os_ms, os_launches = stages["onesweep"]
+    avg_pass_ms = os_ms / max(os_launches, 1)
+    pass_bytes = 2 * (8 + 4) * n
+    achieved = pass_bytes / (avg_pass_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_hbm_peak()
+    traffic = None
+    tp = os.path.join(REPO, "profiles", "onesweep_traffic.json")
+    if os.path.exists(tp):
+        try:
+            tj = json.load(open(tp))
+            traffic = tj["dram_bytes_per_launch_per_key_u64"] * n
+        except Exception:
+            traffic = None
+    alg = algorithmic_bytes(n, u, m, o, 8)
+    alg_total = sum(alg.values())
+    ms_per_step = elapsed_ms / args.steps
+    value = world * n / (ms_per_step * 1e-3) / 1e6
+    kernels_per_step = 1 + 8 + 1 + 1 + 1 + 1  # morton+hist, 8 passes, unique, tree, scan, octree
+    stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
+
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
+                   "onesweep_passes": 8, "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
+                   "n_oct_nodes": o, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (160 MB of points, ~1 GB working set per build)",
+                   "graph_ms_per_step": round(graph_ms, 4), "stage_ms_per_step": stage_ms,
+                   "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
+                   "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
+                   "sort_variant": ctx.get_sort_variant(64)},
+        "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_launch": pass_bytes, "avg_launch_ms": round(avg_pass_ms, 5)},
+        "e2e": {"value": round(n / e2e_s / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                "d2h_bytes_per_step": o * 64 + 16, "api": "gtc_build_octree_host (pinned host buffers)"},
+        "gpu_launches": kernels_per_step * args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pts_np)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def cpu_baseline(pts_np):
+    import oracle
+
+    oracle.build()
+    threads = cpu_threads()
+    reps = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.build_octree(pts_np, KEY_BITS, threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= 10.0 or reps >= 8:
+            break
+    n = pts_np.shape[0]
+    return {"value": round(n * reps / el / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} full builds of the same {n}-point cloud with the oracle ({threads} threads)"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gtc(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,242 @@
+// gtc_internal.cuh - shared device helpers and launcher declarations.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gtc.h"
+
+namespace gtc {
+
+// Bits of the device status word (ctx-owned, read by gtc_device_status).
+constexpr uint32_t DEV_TIMEOUT = 1u;   // a bounded spin ran out
+constexpr uint32_t DEV_CAPACITY = 2u;  // an output buffer was too small
+constexpr uint32_t DEV_INTERNAL = 4u;  // an impossible state was detected
+
+// Descriptor flags for decoupled look-back: value << 2 | flag.
+constexpr uint32_t FLAG_NOT_READY = 0u;
+constexpr uint32_t FLAG_AGGREGATE = 1u;
+constexpr uint32_t FLAG_INCLUSIVE = 2u;
+
+// Spins poll at most this many times (with __nanosleep backoff after the
+// first few), i.e. well under a second, before giving up with DEV_TIMEOUT.
+constexpr uint32_t SPIN_LIMIT = 1u << 20;
+
+constexpr int NUM_SMS_GB300 = 152;
+
+template <class K>
+struct KeyTraits;
+template <>
+struct KeyTraits<uint32_t> {
+  static constexpr int W = 32;
+  static constexpr int B = 10;   // bits per axis
+  static constexpr int A = 2;    // unused high bits
+};
+template <>
+struct KeyTraits<uint64_t> {
+  static constexpr int W = 64;
+  static constexpr int B = 21;
+  static constexpr int A = 1;
+};
+
+__device__ __forceinline__ int clz_key(uint32_t x) { return __clz(x); }
+__device__ __forceinline__ int clz_key(uint64_t x) { return __clzll(x); }
+
+// delta(a, b) of build_radix_tree.comp:48-58: leading common bits, W if equal.
+template <class K>
+__device__ __forceinline__ int delta_key(K a, K b) {
+  const K x = a ^ b;
+  return x == 0 ? KeyTraits<K>::W : clz_key(x);
+}
+
+// ----------------------------------------------------------- relaxed I/O --
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until *p carries a flag, at most SPIN_LIMIT polls.  On expiry records
+// DEV_TIMEOUT and returns an INCLUSIVE descriptor of value 0 so the caller's
+// look-back ends.
+__device__ __forceinline__ uint32_t spin_descriptor(const uint32_t* p, uint32_t* status) {
+  uint32_t v = ld_relaxed(p);
+  uint32_t it = 0;
+  while ((v & 3u) == FLAG_NOT_READY) {
+    if (++it > SPIN_LIMIT) {
+      atomicOr(status, DEV_TIMEOUT);
+      return FLAG_INCLUSIVE;
+    }
+    if (it > 16) __nanosleep(32);
+    v = ld_relaxed(p);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------- morton --
+// D17 saturating conversion, identical to the oracle's.
+__device__ __forceinline__ uint32_t f2u_sat(float a) {
+  if (!(a > 0.0f)) return 0u;
+  if (a >= 4294967296.0f) return 0xFFFFFFFFu;
+  return __float2uint_rz(a);
+}
+
+// morton.comp:50-56: (v - min) / range, then * 2^B, each op rounded to nearest.
+__device__ __forceinline__ uint32_t quantize(float v, float mn, float rg, float scale) {
+  const float t = __fdiv_rn(__fsub_rn(v, mn), rg);
+  return f2u_sat(__fmul_rn(t, scale));
+}
+
+__device__ __forceinline__ uint32_t split3_32(uint32_t b) {  // morton.comp:36-44
+  uint32_t x = b & 0x000003ffu;
+  x = (x | x << 16) & 0x030000ffu;
+  x = (x | x << 8) & 0x0300f00fu;
+  x = (x | x << 4) & 0x030c30c3u;
+  x = (x | x << 2) & 0x09249249u;
+  return x;
+}
+__device__ __forceinline__ uint64_t split3_64(uint32_t b) {
+  uint64_t x = b & 0x1fffffull;
+  x = (x | x << 32) & 0x001f00000000ffffull;
+  x = (x | x << 16) & 0x001f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+__device__ __forceinline__ uint32_t third_bits(uint32_t m) {  // morton.rs:62-68
+  uint32_t x = m & 0x09249249u;
+  x = (x ^ (x >> 2)) & 0x030c30c3u;
+  x = (x ^ (x >> 4)) & 0x0300f00fu;
+  x = (x ^ (x >> 8)) & 0x030000ffu;
+  x = (x ^ (x >> 16)) & 0x000003ffu;
+  return x;
+}
+__device__ __forceinline__ uint32_t third_bits(uint64_t m) {
+  uint64_t x = m & 0x1249249249249249ull;
+  x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
+  x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
+  x = (x ^ (x >> 8)) & 0x001f0000ff0000ffull;
+  x = (x ^ (x >> 16)) & 0x001f00000000ffffull;
+  x = (x ^ (x >> 32)) & 0x00000000001fffffull;
+  return (uint32_t)x;
+}
+
+template <class K>
+__device__ __forceinline__ K encode_point(float4 p, float mn, float rg);
+template <>
+__device__ __forceinline__ uint32_t encode_point<uint32_t>(float4 p, float mn, float rg) {
+  return split3_32(quantize(p.x, mn, rg, 1024.0f)) | (split3_32(quantize(p.y, mn, rg, 1024.0f)) << 1) |
+         (split3_32(quantize(p.z, mn, rg, 1024.0f)) << 2);
+}
+template <>
+__device__ __forceinline__ uint64_t encode_point<uint64_t>(float4 p, float mn, float rg) {
+  const float s = 2097152.0f;
+  return split3_64(quantize(p.x, mn, rg, s)) | (split3_64(quantize(p.y, mn, rg, s)) << 1) |
+         (split3_64(quantize(p.z, mn, rg, s)) << 2);
+}
+
+// morton32_to_xyz (morton.rs:43-60): (q / 2^B) * range + min, no contraction.
+template <class K>
+__device__ __forceinline__ float4 decode_corner(K code, float mn, float rg) {
+  const float bs = (KeyTraits<K>::B == 10) ? 1024.0f : 2097152.0f;
+  float4 r;
+  r.x = __fadd_rn(__fmul_rn(__fdiv_rn((float)third_bits(code), bs), rg), mn);
+  r.y = __fadd_rn(__fmul_rn(__fdiv_rn((float)third_bits((K)(code >> 1)), bs), rg), mn);
+  r.z = __fadd_rn(__fmul_rn(__fdiv_rn((float)third_bits((K)(code >> 2)), bs), rg), mn);
+  r.w = 1.0f;
+  return r;
+}
+
+// ----------------------------------------------------------- warp scans ---
+__device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// ------------------------------------------------------- launcher table ---
+struct Launch {
+  cudaStream_t stream;
+  uint32_t* status;  // device status word
+  int num_sms;
+};
+
+// Sort tuning knobs, chosen from the compiled variant table.
+struct SortConfig {
+  int threads;
+  int kpt;
+  int variant;  // index into the compiled table
+};
+
+// Workspace layout of a sort of n keys with `passes` 8-bit passes.
+struct SortWorkspace {
+  uint32_t* header;       // done counter, tile counters[passes]
+  uint32_t* counts;       // [passes][256]
+  uint32_t* bin_offsets;  // [passes][256]
+  uint32_t* desc;         // [passes][tiles][256]
+  size_t header_words;    // words zeroed per call (header + counts)
+  size_t desc_words;
+  uint32_t tiles;
+};
+
+size_t sort_workspace_bytes(uint32_t n, int passes, int tile_keys);
+SortWorkspace carve_sort_workspace(void* ws, uint32_t n, int passes, int tile_keys);
+
+// Kernels' host launchers (morton.cu / onesweep.cu / scan.cu / tree.cu / octree.cu).
+cudaError_t launch_morton32(const Launch& L, const float4* pts, uint32_t* keys, uint32_t* idx, uint32_t n, float mn,
+                            float rg);
+cudaError_t launch_morton64(const Launch& L, const float4* pts, uint64_t* keys, uint32_t* idx, uint32_t n, float mn,
+                            float rg);
+// Fused Morton encode + iota + global histogram for a following sort.
+template <class K>
+cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t* idx, uint32_t n, float mn,
+                               float rg, const SortWorkspace& W, int passes);
+
+template <class K>
+cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
+                               const SortWorkspace& W, int passes);
+template <class K>
+int sort_tile_keys(uint32_t n);
+template <class K>
+cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
+                                   uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
+                                   bool* result_in_alt, cudaEvent_t* ev_pass /* nullable [2*passes] */);
+
+// Decoupled look-back scans: unique compaction and node offsets.
+size_t scan_workspace_bytes(uint32_t n);
+template <class K>
+cudaError_t launch_unique(const Launch& L, const K* keys_in, const uint32_t* vals_in, K* keys_out,
+                          uint32_t* vals_out, uint32_t n, uint32_t* d_count, void* ws);
+cudaError_t launch_inclusive_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t n, void* ws);
+// Node offsets over u = m + 1 entries, m = (d_u ? *d_u - 1 : m_host).
+cudaError_t launch_node_offsets(const Launch& L, const uint32_t* edge, uint32_t* ps, const uint32_t* d_u,
+                                uint32_t m_host, uint32_t n_max, uint32_t* d_o, void* ws);
+
+template <class K>
+cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d_u, int32_t m_host, uint32_t n_max,
+                              uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int32_t* left, int32_t* parent,
+                              uint32_t* edge, uint32_t* d_m /* nullable: receives m */);
+cudaError_t launch_edge_count(const Launch& L, const uint8_t* prefix_n, const int32_t* parent, uint32_t* edge,
+                              uint32_t m, int unused_bits);
+template <class K>
+cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* d_u, uint32_t u_host,
+                               uint32_t n_max, const uint8_t* prefix_n, const uint8_t* hll, const uint8_t* hlr,
+                               const int32_t* left, const uint32_t* edge, const uint32_t* ps, float mn, float rg,
+                               gtc_octnode* nodes, uint32_t capacity, bool with_leaves);
+template <class K>
+cudaError_t launch_octree_link(const Launch& L, const K* codes, uint32_t m, const uint8_t* prefix_n,
+                               const uint8_t* hll, const uint8_t* hlr, const int32_t* left, const int32_t* parent,
+                               const uint32_t* edge, const uint32_t* ps, gtc_octnode* nodes, uint32_t capacity);
+
+inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace gtc

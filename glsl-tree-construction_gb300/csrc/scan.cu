@@ -1,0 +1,272 @@
+// scan.cu - single-pass decoupled look-back scans: unique compaction and the
+// octree node-offset scan.
+//
+// unique.comp:31-49 and partial_sum.comp:23-39 run on ONE GPU thread
+// (unique.rs:245, partial_sum.rs:246).  Here both are one pass over the data:
+// each tile of THREADS * IPT items (blocked per thread) is staged through
+// shared memory with coalesced loads, reduced, chained to its predecessors by
+// a warp-wide look-back over per-tile descriptors, and written back with
+// coalesced stores.
+
+#include "gtc_internal.cuh"
+
+namespace gtc {
+
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_IPT = 9;  // odd: conflict-free blocked reads of 32-bit words
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_IPT;
+
+// Workspace: [0] tile counter, [1..63] spare, [64..64+tiles) descriptors.
+size_t scan_workspace_bytes(uint32_t n) {
+  const uint32_t tiles = ceil_div(n > 0 ? n : 1, SCAN_TILE) + 1;
+  return align_up((64 + (size_t)tiles) * 4, 256);
+}
+
+// Block-wide exclusive scan of one value per thread.  Returns the prefix and
+// the block total.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+  constexpr int WARPS = THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const uint32_t incl = warp_inclusive_sum(v);
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = (lane < WARPS) ? warp_sums[lane] : 0u;
+    const uint32_t wi = warp_inclusive_sum(w);
+    if (lane < WARPS) warp_sums[lane] = wi - w;
+    if (lane == WARPS - 1) warp_sums[WARPS] = wi;
+  }
+  __syncthreads();
+  *total = warp_sums[WARPS];
+  return warp_sums[warp] + incl - v;
+}
+
+// Warp 0 chains this tile to its predecessors.  Publishes the aggregate,
+// looks back over a 32-tile window at a time and publishes the inclusive
+// prefix.  Returns the exclusive prefix of the tile (valid in lane 0..31).
+__device__ __forceinline__ uint32_t tile_lookback(uint32_t* desc, uint32_t tile, uint32_t aggregate,
+                                                  uint32_t* status) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {
+    if (lane == 0) st_relaxed(desc, (aggregate << 2) | FLAG_INCLUSIVE);
+    return 0;
+  }
+  if (lane == 0) st_relaxed(desc + tile, (aggregate << 2) | FLAG_AGGREGATE);
+  uint32_t excl = 0;
+  int k = (int)tile - 1 - lane;
+  while (true) {
+    const uint32_t v = (k >= 0) ? spin_descriptor(desc + k, status) : FLAG_INCLUSIVE;
+    const uint32_t incl_mask = __ballot_sync(0xffffffffu, (v & 3u) == FLAG_INCLUSIVE);
+    uint32_t contrib = v >> 2;
+    if (incl_mask) {
+      const int first = __ffs(incl_mask) - 1;  // closest inclusive predecessor
+      if (lane > first) contrib = 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+    excl += contrib;
+    if (incl_mask) break;
+    k -= 32;
+  }
+  if (lane == 0) st_relaxed(desc + tile, ((excl + aggregate) << 2) | FLAG_INCLUSIVE);
+  return excl;
+}
+
+// ---------------------------------------------------------------- unique --
+template <class K>
+struct UniqueSmem {
+  K keys[SCAN_TILE];
+  uint32_t vals[SCAN_TILE];
+  uint32_t warp_sums[SCAN_THREADS / 32 + 1];
+  uint32_t tile_id;
+  uint32_t prefix;
+  K halo;
+};
+
+template <class K, bool HAS_VALS>
+__global__ void __launch_bounds__(SCAN_THREADS) unique_kernel(const K* kin, const uint32_t* vin, K* kout,
+                                                              uint32_t* vout, uint32_t n, uint32_t* ws,
+                                                              uint32_t* d_count, uint32_t* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  UniqueSmem<K>& s = *reinterpret_cast<UniqueSmem<K>*>(smem_raw);
+  uint32_t* desc = ws + 64;
+  const int tid = threadIdx.x;
+  if (tid == 0) s.tile_id = atomicAdd(ws, 1u);
+  __syncthreads();
+  const uint32_t tile = s.tile_id;
+  const uint32_t base = tile * SCAN_TILE;
+  if (base >= n) return;  // no tile is ever launched past n by the launcher
+  const uint32_t valid = min((uint32_t)SCAN_TILE, n - base);
+  // Every read of this tile's input (and the halo) happens before the tile
+  // publishes its aggregate, and every write happens after its look-back
+  // completes, so in-place compaction (kin == kout) is safe.
+  for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
+    s.keys[i] = kin[base + i];
+    if (HAS_VALS) s.vals[i] = vin[base + i];
+  }
+  if (tid == 0) s.halo = (base > 0) ? kin[base - 1] : K(0);
+  __syncthreads();
+  K key[SCAN_IPT];
+  uint32_t val[SCAN_IPT];
+  uint32_t flags = 0, cnt = 0;
+  const uint32_t first = tid * SCAN_IPT;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    const uint32_t i = first + j;
+    if (i < valid) {
+      key[j] = s.keys[i];
+      if (HAS_VALS) val[j] = s.vals[i];
+      const K prev = (i == 0) ? s.halo : s.keys[i - 1];
+      const bool keep = (base + i == 0) || (key[j] != prev);
+      flags |= (uint32_t)keep << j;
+      cnt += keep;
+    }
+  }
+  uint32_t total;
+  const uint32_t excl = block_exclusive<SCAN_THREADS>(cnt, s.warp_sums, &total);
+  if (tid < 32) {
+    const uint32_t pre = tile_lookback(desc, tile, total, status);
+    if (tid == 0) s.prefix = pre;
+  }
+  __syncthreads();  // also: everyone is done reading s.keys / s.vals
+  uint32_t r = excl;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    if (flags & (1u << j)) {
+      s.keys[r] = key[j];
+      if (HAS_VALS) s.vals[r] = val[j];
+      ++r;
+    }
+  }
+  __syncthreads();
+  const uint32_t out = s.prefix;
+  for (uint32_t i = tid; i < total; i += SCAN_THREADS) {
+    kout[out + i] = s.keys[i];
+    if (HAS_VALS) vout[out + i] = s.vals[i];
+  }
+  if (tid == 0 && base + valid == n && d_count) *d_count = out + total;
+}
+
+template <class K>
+cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout, uint32_t n,
+                          uint32_t* d_count, void* ws) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(ws);
+  const uint32_t tiles = ceil_div(n, SCAN_TILE);
+  cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return d_count ? cudaMemsetAsync(d_count, 0, 4, L.stream) : cudaSuccess;
+  const size_t smem = sizeof(UniqueSmem<K>);
+  static bool attr_set[2] = {false, false};  // per instantiation: set once, outside any graph capture
+  if (vin) {
+    auto kern = unique_kernel<K, true>;
+    if (!attr_set[1]) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      attr_set[1] = true;
+    }
+    kern<<<tiles, SCAN_THREADS, smem, L.stream>>>(kin, vin, kout, vout, n, w, d_count, L.status);
+  } else {
+    auto kern = unique_kernel<K, false>;
+    if (!attr_set[0]) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      attr_set[0] = true;
+    }
+    kern<<<tiles, SCAN_THREADS, smem, L.stream>>>(kin, nullptr, kout, nullptr, n, w, d_count, L.status);
+  }
+  return cudaGetLastError();
+}
+template cudaError_t launch_unique<uint32_t>(const Launch&, const uint32_t*, const uint32_t*, uint32_t*, uint32_t*,
+                                             uint32_t, uint32_t*, void*);
+template cudaError_t launch_unique<uint64_t>(const Launch&, const uint64_t*, const uint32_t*, uint64_t*, uint32_t*,
+                                             uint32_t, uint32_t*, void*);
+
+// ------------------------------------------------------------------ scan --
+// Inclusive scan of `count` elements; element k reads in[k] when k < limit,
+// else 0.  With node_offsets set: count = u = *d_u (or host), limit = u - 1,
+// out[0] forced to 0 and *d_o = 1 + out[u - 1] (main.rs:127-129; D4).
+struct ScanSmem {
+  uint32_t vals[SCAN_TILE];
+  uint32_t warp_sums[SCAN_THREADS / 32 + 1];
+  uint32_t tile_id;
+  uint32_t prefix;
+};
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(const uint32_t* in, uint32_t* out, uint32_t count_host,
+                                                            const uint32_t* d_u, int node_offsets, uint32_t* ws,
+                                                            uint32_t* d_o, uint32_t* status) {
+  __shared__ ScanSmem s;
+  uint32_t* desc = ws + 64;
+  const int tid = threadIdx.x;
+  const uint32_t count = d_u ? *d_u : count_host;
+  const uint32_t limit = node_offsets ? (count > 0 ? count - 1 : 0) : count;
+  if (tid == 0) s.tile_id = atomicAdd(ws, 1u);
+  __syncthreads();
+  const uint32_t tile = s.tile_id;
+  const uint32_t base = tile * SCAN_TILE;
+  if (base >= count) {
+    if (node_offsets && count == 0 && tile == 0 && tid == 0 && d_o) *d_o = 0;
+    return;
+  }
+  const uint32_t valid = min((uint32_t)SCAN_TILE, count - base);
+  for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
+    const uint32_t g = base + i;
+    s.vals[i] = (g < limit) ? in[g] : 0u;
+  }
+  __syncthreads();
+  uint32_t v[SCAN_IPT];
+  uint32_t sum = 0;
+  const uint32_t first = tid * SCAN_IPT;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    v[j] = (first + j < valid) ? s.vals[first + j] : 0u;
+    sum += v[j];
+  }
+  uint32_t total;
+  const uint32_t excl = block_exclusive<SCAN_THREADS>(sum, s.warp_sums, &total);
+  if (tid < 32) {
+    const uint32_t pre = tile_lookback(desc, tile, total, status);
+    if (tid == 0) s.prefix = pre;
+  }
+  __syncthreads();
+  uint32_t run = s.prefix + excl;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    run += v[j];
+    if (first + j < valid) s.vals[first + j] = run;
+  }
+  __syncthreads();
+  for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
+    const uint32_t g = base + i;
+    out[g] = (node_offsets && g == 0) ? 0u : s.vals[i];
+  }
+  if (node_offsets && tid == 0 && base + valid == count && d_o) {
+    const uint32_t last = (count == 1) ? 0u : s.prefix + total;
+    *d_o = 1 + last;
+  }
+}
+
+static cudaError_t launch_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t count_host,
+                               const uint32_t* d_u, uint32_t n_max, int node_offsets, uint32_t* d_o, void* ws) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(ws);
+  const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);
+  cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
+  if (e != cudaSuccess) return e;
+  scan_kernel<<<tiles, SCAN_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inclusive_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t n, void* ws) {
+  if (n == 0) return cudaSuccess;
+  return launch_scan(L, in, out, n, nullptr, n, 0, nullptr, ws);
+}
+
+cudaError_t launch_node_offsets(const Launch& L, const uint32_t* edge, uint32_t* ps, const uint32_t* d_u,
+                                uint32_t m_host, uint32_t n_max, uint32_t* d_o, void* ws) {
+  // u = m + 1 entries; with d_u the count comes from the device (<= n_max).
+  return launch_scan(L, edge, ps, m_host + 1, d_u, d_u ? n_max : m_host + 1, 1, d_o, ws);
+}
+
+}  // namespace gtc

@@ -1,0 +1,432 @@
+// sort.cu - global digit histogram and onesweep LSD digit-binning passes.
+//
+// Replaces histogram.comp:103-195 (upfront histogram) and
+// new_radix_sort.comp:116-314 (one onesweep pass) driven by
+// test_radix_sort (radixsort-vulkan/src/main.rs:175-800), with a u32 payload
+// carried alongside the keys and 8-bit digits over [begin_bit, end_bit).
+//
+// One pass over a tile of TILE = THREADS * KPT keys:
+//   1. tile ticket from an atomic counter (tiles start in ticket order, so a
+//      tile only ever waits on tiles that are already running);
+//   2. warp-striped coalesced loads (lane l of warp w holds keys
+//      w*32*KPT + j*32 + l), padding past n with all-ones keys (max digit);
+//   3. warp-level multisplit: 8 __ballot_sync per key give the peer mask of
+//      lanes with the same digit; ranks follow original order (stable);
+//   4. per-digit counts published as AGGREGATE descriptors [tile][digit];
+//   5. decoupled look-back, one thread per digit, bounded spins;
+//   6. scatter into shared memory in tile-local digit order, then coalesced
+//      writes of each digit run to its global position.
+
+#include <cstdio>
+
+#include "gtc_internal.cuh"
+
+namespace gtc {
+
+constexpr int RADIX = 256;
+constexpr int MAX_PASSES = 8;
+
+// ----------------------------------------------------- block-level helpers --
+// Exclusive scan of one value per thread over the first 256 threads (warps
+// 0..7); every thread of the block must call it.  Returns the exclusive
+// prefix for threads < 256.
+template <int THREADS>
+__device__ __forceinline__ uint32_t scan256_exclusive(uint32_t v, uint32_t* warp_sums /*[8]*/) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  uint32_t incl = 0;
+  if (tid < RADIX) {
+    incl = warp_inclusive_sum(v);
+    if (lane == 31) warp_sums[warp] = incl;
+  }
+  __syncthreads();
+  uint32_t pre = 0;
+  if (tid < RADIX) {
+#pragma unroll
+    for (int w = 0; w < RADIX / 32; ++w) pre += (w < warp) ? warp_sums[w] : 0u;
+  }
+  return pre + incl - v;
+}
+
+// ------------------------------------------------------ global histogram ---
+template <class K>
+__device__ __forceinline__ void hist_add(uint32_t (*s_hist)[RADIX], K k, int begin_bit, int end_bit, int passes) {
+#pragma unroll
+  for (int p = 0; p < MAX_PASSES; ++p) {
+    if (p < passes) {
+      const int sh = begin_bit + 8 * p;
+      const int bits = min(8, end_bit - sh);
+      const uint32_t d = (uint32_t)(k >> sh) & ((1u << bits) - 1u);
+      atomicAdd(&s_hist[p][d], 1u);
+    }
+  }
+}
+
+// Adds the block's shared histograms into the global counts; the last block
+// to finish turns the counts into exclusive prefixes (bin offsets) and resets
+// the done counter, so the workspace needs no clearing between calls.
+template <int THREADS>
+__device__ __forceinline__ void hist_finish(uint32_t (*s_hist)[RADIX], int passes, uint32_t* counts,
+                                            uint32_t* bin_offsets, uint32_t* done, uint32_t* s_warp_sums,
+                                            uint32_t* s_last) {
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * RADIX; i += THREADS) {
+    const uint32_t c = (&s_hist[0][0])[i];
+    if (c) atomicAdd(&counts[i], c);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *s_last = (atomicAdd(done, 1u) == gridDim.x - 1) ? 1u : 0u;
+  __syncthreads();
+  if (*s_last == 0) return;
+  __threadfence();
+  for (int p = 0; p < passes; ++p) {
+    const uint32_t c = (threadIdx.x < RADIX) ? __ldcg(&counts[p * RADIX + threadIdx.x]) : 0u;
+    const uint32_t ex = scan256_exclusive<THREADS>(c, s_warp_sums);
+    if (threadIdx.x < RADIX) bin_offsets[p * RADIX + threadIdx.x] = ex;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *done = 0;
+}
+
+__device__ __forceinline__ void zero_region(uint32_t* p, size_t words) {
+  // Grid-stride zeroing of a 16-byte aligned region (next sort's descriptors).
+  const size_t n4 = words / 4;
+  uint4* p4 = reinterpret_cast<uint4*>(p);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) p4[i] = make_uint4(0, 0, 0, 0);
+  for (size_t i = n4 * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) p[i] = 0;
+}
+
+template <class K, int THREADS>
+__global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restrict__ keys, uint32_t n, int begin_bit,
+                                                              int end_bit, int passes, uint32_t* counts,
+                                                              uint32_t* bin_offsets, uint32_t* done,
+                                                              uint32_t* zero_ptr, size_t zero_words) {
+  __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
+  __shared__ uint32_t s_warp_sums[8];
+  __shared__ uint32_t s_last;
+  for (int i = threadIdx.x; i < MAX_PASSES * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
+  zero_region(zero_ptr, zero_words);
+  __syncthreads();
+  const size_t stride = (size_t)gridDim.x * THREADS;
+  constexpr int VEC = 16 / sizeof(K);
+  const bool aligned = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+  const uint32_t nvec = aligned ? n / VEC : 0;
+  for (size_t v = (size_t)blockIdx.x * THREADS + threadIdx.x; v < nvec; v += stride) {
+    const uint4 q = __ldcs(reinterpret_cast<const uint4*>(keys) + v);
+    const K* kk = reinterpret_cast<const K*>(&q);
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) hist_add<K>(s_hist, kk[e], begin_bit, end_bit, passes);
+  }
+  for (size_t i = (size_t)nvec * VEC + (size_t)blockIdx.x * THREADS + threadIdx.x; i < n; i += stride)
+    hist_add<K>(s_hist, keys[i], begin_bit, end_bit, passes);
+  hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, s_warp_sums, &s_last);
+}
+
+// Fused Morton encode + iota payload + global histogram: the first stage of
+// the pipeline reads the points once and leaves the sort ready to run.
+template <class K, int THREADS>
+__global__ void __launch_bounds__(THREADS) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
+                                                              uint32_t* __restrict__ idx, uint32_t n, float mn,
+                                                              float rg, int end_bit, int passes, uint32_t* counts,
+                                                              uint32_t* bin_offsets, uint32_t* done,
+                                                              uint32_t* zero_ptr, size_t zero_words) {
+  __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
+  __shared__ uint32_t s_warp_sums[8];
+  __shared__ uint32_t s_last;
+  for (int i = threadIdx.x; i < MAX_PASSES * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
+  zero_region(zero_ptr, zero_words);
+  __syncthreads();
+  const size_t stride = (size_t)gridDim.x * THREADS;
+  for (size_t i = (size_t)blockIdx.x * THREADS + threadIdx.x; i < n; i += stride) {
+    const float4 p = __ldcs(pts + i);
+    const K k = encode_point<K>(p, mn, rg);
+    keys[i] = k;
+    idx[i] = (uint32_t)i;
+    hist_add<K>(s_hist, k, 0, end_bit, passes);
+  }
+  hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, s_warp_sums, &s_last);
+}
+
+// ------------------------------------------------------------ onesweep ----
+template <class K, int THREADS, int KPT>
+struct OnesweepSmem {
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int TILE = THREADS * KPT;
+  K keys[TILE];
+  uint32_t vals[TILE];
+  uint32_t warp_hist[WARPS][RADIX];
+  uint32_t digit_offset[RADIX];
+  uint32_t global_base[RADIX];
+  uint32_t warp_sums[8];
+  uint32_t tile_id;
+};
+
+template <class K, int THREADS, int KPT, bool HAS_VALS>
+__global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                           K* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, int shift, uint32_t dmask,
+                                                           const uint32_t* __restrict__ bin_off,
+                                                           uint32_t* __restrict__ desc,
+                                                           uint32_t* __restrict__ tile_counter,
+                                                           uint32_t* __restrict__ status) {
+  using S = OnesweepSmem<K, THREADS, KPT>;
+  constexpr int WARPS = S::WARPS;
+  constexpr int TILE = S::TILE;
+  static_assert(THREADS >= RADIX, "one thread per digit");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S& s = *reinterpret_cast<S*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+
+  for (int i = tid; i < WARPS * RADIX; i += THREADS) (&s.warp_hist[0][0])[i] = 0;
+  if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s.tile_id;
+  const uint32_t tile_base = tile * TILE;
+
+  // 2. warp-striped coalesced loads.
+  K key[KPT];
+  uint32_t val[KPT];
+  const uint32_t wbase = tile_base + warp * 32 * KPT + lane;
+#pragma unroll
+  for (int j = 0; j < KPT; ++j) {
+    const uint32_t pos = wbase + j * 32;
+    key[j] = (pos < n) ? kin[pos] : ~K(0);
+    if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
+  }
+
+  // 3. warp multisplit ranks (stable: j-major then lane order = input order).
+  uint32_t rank[KPT];
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t* my_hist = s.warp_hist[warp];
+#pragma unroll
+  for (int j = 0; j < KPT; ++j) {
+    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint32_t bit = (d >> b) & 1u;
+      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? bal : ~bal;
+    }
+    const uint32_t base = my_hist[d];
+    __syncwarp();
+    if (lane == 31 - __clz(peers)) my_hist[d] = base + __popc(peers);
+    __syncwarp();
+    rank[j] = base + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+
+  // 4. per-digit counts across warps; publish the tile aggregate early.
+  uint32_t count = 0;
+  if (tid < RADIX) {
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t c = s.warp_hist[w][tid];
+      s.warp_hist[w][tid] = count;
+      count += c;
+    }
+    st_relaxed(desc + (size_t)tile * RADIX + tid, (count << 2) | (tile == 0 ? FLAG_INCLUSIVE : FLAG_AGGREGATE));
+  }
+  const uint32_t digit_off = scan256_exclusive<THREADS>(count, s.warp_sums);
+
+  // 5. decoupled look-back over predecessor tiles, one thread per digit.
+  if (tid < RADIX) {
+    s.digit_offset[tid] = digit_off;
+    uint32_t excl = 0;
+    if (tile > 0) {
+      int k = (int)tile - 1;
+      while (true) {
+        const uint32_t v = spin_descriptor(desc + (size_t)k * RADIX + tid, status);
+        excl += v >> 2;
+        if ((v & 3u) == FLAG_INCLUSIVE || k == 0) break;
+        --k;
+      }
+      st_relaxed(desc + (size_t)tile * RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
+    }
+    s.global_base[tid] = bin_off[tid] + excl - digit_off;
+  }
+  __syncthreads();
+
+  // 6. scatter into tile-local digit order, then coalesced run writes.
+#pragma unroll
+  for (int j = 0; j < KPT; ++j) {
+    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+    const uint32_t local = s.digit_offset[d] + my_hist[d] + rank[j];
+    s.keys[local] = key[j];
+    if (HAS_VALS) s.vals[local] = val[j];
+  }
+  __syncthreads();
+  const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+  for (uint32_t i = tid; i < valid; i += THREADS) {
+    const K k = s.keys[i];
+    const uint32_t o = s.global_base[(uint32_t)(k >> shift) & dmask] + i;
+    kout[o] = k;
+    if (HAS_VALS) vout[o] = s.vals[i];
+  }
+}
+
+// ------------------------------------------------------------- variants ---
+// Tile shapes compiled in.  The first entry per key width is the default;
+// others are available to the autotuner (gtc_sort_set_variant).
+struct Variant {
+  int threads;
+  int kpt;
+};
+constexpr Variant kVariants[] = {{256, 16}, {384, 16}, {512, 12}};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+static int g_variant[2] = {0, 0};  // [u32, u64]
+
+template <class K, int THREADS, int KPT, bool HV>
+static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
+                              uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
+                              uint32_t* tile_counter) {
+  using S = OnesweepSmem<K, THREADS, KPT>;
+  auto kern = onesweep_kernel<K, THREADS, KPT, HV>;
+  static bool attr_set = false;  // per instantiation
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const uint32_t tiles = ceil_div(n, S::TILE);
+  kern<<<tiles, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
+                                                L.status);
+  return cudaGetLastError();
+}
+
+template <class K>
+static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin, const uint32_t* vin, K* kout,
+                                  uint32_t* vout, uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off,
+                                  uint32_t* desc, uint32_t* tc) {
+#define GTC_OS(T, P)                                                                                     \
+  return hv ? launch_one<K, T, P, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)   \
+            : launch_one<K, T, P, false>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+  switch (v) {
+    case 0: GTC_OS(256, 16);
+    case 1: GTC_OS(384, 16);
+    default: GTC_OS(512, 12);
+  }
+#undef GTC_OS
+}
+
+template <class K>
+int sort_tile_keys(uint32_t) {
+  const Variant& v = kVariants[g_variant[sizeof(K) == 8]];
+  return v.threads * v.kpt;
+}
+template int sort_tile_keys<uint32_t>(uint32_t);
+template int sort_tile_keys<uint64_t>(uint32_t);
+
+// Smallest tile of any variant: sizes the descriptor array for every variant.
+static int min_tile_keys() {
+  int t = 1 << 30;
+  for (const Variant& v : kVariants) t = t < v.threads * v.kpt ? t : v.threads * v.kpt;
+  return t;
+}
+
+size_t sort_workspace_bytes(uint32_t n, int passes, int /*tile_keys*/) {
+  const uint32_t tiles = ceil_div(n > 0 ? n : 1, (uint32_t)min_tile_keys());
+  size_t words = 64 + 2 * (size_t)MAX_PASSES * RADIX;  // header + counts + bin offsets
+  words = align_up(words, 64);
+  words += (size_t)passes * tiles * RADIX;
+  return align_up(words * 4, 256);
+}
+
+SortWorkspace carve_sort_workspace(void* ws, uint32_t n, int passes, int /*tile_keys*/) {
+  SortWorkspace W;
+  uint32_t* p = reinterpret_cast<uint32_t*>(ws);
+  W.tiles = ceil_div(n > 0 ? n : 1, (uint32_t)min_tile_keys());
+  W.header = p;                              // [0] done, [1..8] tile counters
+  W.counts = p + 64;                         // [passes][256]
+  W.bin_offsets = p + 64 + MAX_PASSES * RADIX;
+  W.header_words = 64 + (size_t)MAX_PASSES * RADIX;  // header + counts zeroed per call
+  const size_t desc_off = align_up(64 + 2 * (size_t)MAX_PASSES * RADIX, 64);
+  W.desc = p + desc_off;
+  W.desc_words = (size_t)passes * W.tiles * RADIX;
+  return W;
+}
+
+template <class K>
+cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
+                               const SortWorkspace& W, int passes) {
+  constexpr int T = 512;
+  const uint32_t want = ceil_div(n, T * 16);
+  const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 2));
+  global_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(keys, n, begin_bit, end_bit, passes, W.counts, W.bin_offsets,
+                                                     W.header, W.desc, W.desc_words);
+  return cudaGetLastError();
+}
+template cudaError_t launch_global_hist<uint32_t>(const Launch&, const uint32_t*, uint32_t, int, int,
+                                                  const SortWorkspace&, int);
+template cudaError_t launch_global_hist<uint64_t>(const Launch&, const uint64_t*, uint32_t, int, int,
+                                                  const SortWorkspace&, int);
+
+template <class K>
+cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t* idx, uint32_t n, float mn,
+                               float rg, const SortWorkspace& W, int passes) {
+  constexpr int T = 512;
+  const uint32_t want = ceil_div(n, T * 8);
+  const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 2));
+  morton_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(pts, keys, idx, n, mn, rg, 3 * KeyTraits<K>::B, passes,
+                                                     W.counts, W.bin_offsets, W.header, W.desc, W.desc_words);
+  return cudaGetLastError();
+}
+template cudaError_t launch_morton_hist<uint32_t>(const Launch&, const float4*, uint32_t*, uint32_t*, uint32_t, float,
+                                                  float, const SortWorkspace&, int);
+template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, uint64_t*, uint32_t*, uint32_t, float,
+                                                  float, const SortWorkspace&, int);
+
+template <class K>
+cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
+                                   uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
+                                   bool* result_in_alt, cudaEvent_t* ev) {
+  const int v = g_variant[sizeof(K) == 8];
+  const bool hv = vals != nullptr;
+  K* src_k = keys;
+  K* dst_k = keys_alt;
+  uint32_t* src_v = vals;
+  uint32_t* dst_v = vals_alt;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = begin_bit + 8 * p;
+    const int bits = min(8, end_bit - shift);
+    const uint32_t dmask = (1u << bits) - 1u;
+    if (ev) cudaEventRecord(ev[2 * p], L.stream);
+    cudaError_t e = launch_variant<K>(v, hv, L, src_k, src_v, dst_k, dst_v, n, shift, dmask, W.bin_offsets + p * RADIX,
+                                      W.desc + (size_t)p * W.tiles * RADIX, W.header + 1 + p);
+    if (e != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[2 * p + 1], L.stream);
+    K* tk = src_k;
+    src_k = dst_k;
+    dst_k = tk;
+    uint32_t* tv = src_v;
+    src_v = dst_v;
+    dst_v = tv;
+  }
+  *result_in_alt = (passes % 2) == 1;
+  return cudaSuccess;
+}
+template cudaError_t launch_onesweep_passes<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
+                                                      uint32_t, int, int, const SortWorkspace&, int, bool*,
+                                                      cudaEvent_t*);
+template cudaError_t launch_onesweep_passes<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*,
+                                                      uint32_t, int, int, const SortWorkspace&, int, bool*,
+                                                      cudaEvent_t*);
+
+int sort_num_variants() { return kNumVariants; }
+int sort_get_variant(int key_bits) { return g_variant[key_bits == 64]; }
+bool sort_set_variant(int key_bits, int v) {
+  if (v < 0 || v >= kNumVariants) return false;
+  g_variant[key_bits == 64] = v;
+  return true;
+}
+void sort_variant_shape(int v, int* threads, int* kpt) {
+  *threads = kVariants[v].threads;
+  *kpt = kVariants[v].kpt;
+}
+
+}  // namespace gtc

@@ -1,0 +1,324 @@
+"""Python driver of the GB300-native octree-construction library (libgtc.so).
+
+Thin ctypes layer over the C ABI in include/gtc.h.  Device buffers are torch
+CUDA tensors (plumbing only: allocation and streams); every computation runs
+in libgtc.so's CUDA kernels.  Operators mirror the reference's stage functions
+(radixsort-vulkan/src/*.rs): compute_morton, histogram, radix_sort, unique,
+build_radix_tree, edge_count, partial_sum, build_octree.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _build, _lib
+from ._lib import OctreeBuffers
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "OVERFLOW_FALLBACK",
+          6: "UNSUPPORTED", 7: "CAPACITY"}
+OP_SORT_PAIRS, OP_UNIQUE, OP_PARTIAL_SUM, OP_BUILD_OCTREE, OP_GLOBAL_HISTOGRAM = 1, 2, 3, 4, 5
+STAGES = ("morton", "histogram", "onesweep", "unique", "radix_tree", "prefix_sum", "octree", "learned")
+
+OCTNODE_DTYPE = np.dtype([("children", "<i4", (8,)), ("corner", "<f4", (4,)), ("cell_size", "<f4"),
+                          ("child_node_mask", "<i4"), ("child_leaf_mask", "<i4"), ("_pad", "<i4")])
+
+
+class GtcError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"gtc status {status} ({STATUS.get(status, '?')}): {msg}")
+
+
+def build(**kw) -> str:
+    return _build.build(**kw)
+
+
+def lib():
+    return _lib.load()
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+class Context:
+    """A libgtc context bound to one CUDA device (gtc_create / gtc_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        s = self.L.gtc_create(ctypes.byref(h), device)
+        if s != 0:
+            raise GtcError(s, "gtc_create failed (no CUDA device?)")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gtc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- status ------------------------------------------------------------
+    def check(self, status: int):
+        if status != 0:
+            raise GtcError(status, (self.L.gtc_last_error(self.h) or b"").decode())
+
+    def device_status(self, stream=None) -> int:
+        """Synchronise and return (and clear) the device status; raises on error."""
+        s = self.L.gtc_device_status(self.h, _stream(stream))
+        self.check(s)
+        return s
+
+    def device_status_code(self, stream=None) -> int:
+        return self.L.gtc_device_status(self.h, _stream(stream))
+
+    def set_profiling(self, on: bool):
+        self.check(self.L.gtc_set_profiling(self.h, 1 if on else 0))
+
+    def stage_times(self, reset: bool = True) -> dict:
+        ms = (ctypes.c_float * 8)()
+        n = (ctypes.c_uint32 * 8)()
+        self.check(self.L.gtc_stage_times(self.h, ms, n, 1 if reset else 0))
+        return {STAGES[i]: (ms[i], n[i]) for i in range(8)}
+
+    def workspace_size(self, op: int, n: int, key_bits: int) -> int:
+        b = ctypes.c_size_t()
+        self.check(self.L.gtc_workspace_size(self.h, op, n, key_bits, ctypes.byref(b)))
+        return b.value
+
+    def workspace(self, op: int, n: int, key_bits: int):
+        torch = _torch()
+        nbytes = self.workspace_size(op, n, key_bits)
+        return torch.empty(max(nbytes, 256), dtype=torch.uint8, device=f"cuda:{self.device}")
+
+    # -- stage operators (device tensors, current torch stream) ------------
+    def morton(self, pts, key_bits: int, min_coord: float = 0.0, rng: float = 1024.0, with_idx: bool = True):
+        torch = _torch()
+        n = pts.shape[0]
+        kd = torch.int32 if key_bits == 32 else torch.int64
+        keys = torch.empty(n, dtype=kd, device=pts.device)
+        idx = torch.empty(n, dtype=torch.int32, device=pts.device) if with_idx else None
+        fn = self.L.gtc_morton32 if key_bits == 32 else self.L.gtc_morton64
+        self.check(fn(self.h, _ptr(pts), _ptr(keys), _ptr(idx), n, min_coord, rng, _stream()))
+        return keys, idx
+
+    def global_histogram(self, keys, begin_bit: int, end_bit: int, ws=None):
+        torch = _torch()
+        passes = (end_bit - begin_bit + 7) // 8
+        hist = torch.empty(passes * 256, dtype=torch.int32, device=keys.device)
+        fn = self.L.gtc_global_histogram_u32 if keys.element_size() == 4 else self.L.gtc_global_histogram_u64
+        self.check(fn(self.h, _ptr(keys), keys.numel(), begin_bit, end_bit, _ptr(hist), _ptr(ws),
+                      0 if ws is None else ws.numel(), _stream()))
+        return hist.view(passes, 256)
+
+    def sort_pairs(self, keys, vals=None, begin_bit: int = 0, end_bit: int | None = None, ws=None,
+                   keys_alt=None, vals_alt=None):
+        """Stable onesweep sort in place (result in keys / vals)."""
+        torch = _torch()
+        n = keys.numel()
+        end_bit = keys.element_size() * 8 if end_bit is None else end_bit
+        keys_alt = torch.empty_like(keys) if keys_alt is None else keys_alt
+        if vals is not None and vals_alt is None:
+            vals_alt = torch.empty_like(vals)
+        fn = self.L.gtc_sort_pairs_u32 if keys.element_size() == 4 else self.L.gtc_sort_pairs_u64
+        self.check(fn(self.h, _ptr(keys), _ptr(vals), _ptr(keys_alt), _ptr(vals_alt), n, begin_bit, end_bit,
+                      _ptr(ws), 0 if ws is None else ws.numel(), _stream()))
+        return keys, vals
+
+    def unique(self, keys, vals=None, ws=None):
+        """In-place unique; returns the device count tensor (1 element)."""
+        torch = _torch()
+        cnt = torch.zeros(1, dtype=torch.int32, device=keys.device)
+        fn = self.L.gtc_unique_u32 if keys.element_size() == 4 else self.L.gtc_unique_u64
+        self.check(fn(self.h, _ptr(keys), _ptr(vals), keys.numel(), _ptr(cnt), _ptr(ws),
+                      0 if ws is None else ws.numel(), _stream()))
+        return cnt
+
+    def radix_tree(self, codes, n_brt_nodes: int, with_edge: bool = False):
+        torch = _torch()
+        m = n_brt_nodes
+        dev = codes.device
+        out = dict(prefix_n=torch.zeros(max(m, 1), dtype=torch.uint8, device=dev),
+                   has_leaf_left=torch.zeros(max(m, 1), dtype=torch.uint8, device=dev),
+                   has_leaf_right=torch.zeros(max(m, 1), dtype=torch.uint8, device=dev),
+                   left_child=torch.zeros(max(m, 1), dtype=torch.int32, device=dev),
+                   parent=torch.zeros(max(m, 1), dtype=torch.int32, device=dev))
+        if with_edge:
+            out["edge_count"] = torch.zeros(max(m, 1), dtype=torch.int32, device=dev)
+        fn = self.L.gtc_build_radix_tree_u32 if codes.element_size() == 4 else self.L.gtc_build_radix_tree_u64
+        self.check(fn(self.h, _ptr(codes), m, _ptr(out["prefix_n"]), _ptr(out["has_leaf_left"]),
+                      _ptr(out["has_leaf_right"]), _ptr(out["left_child"]), _ptr(out["parent"]),
+                      _ptr(out.get("edge_count")), _stream()))
+        return {k: v[:m] for k, v in out.items()}
+
+    def edge_count(self, prefix_n, parent, key_bits: int):
+        torch = _torch()
+        m = prefix_n.numel()
+        edge = torch.zeros(max(m, 1), dtype=torch.int32, device=prefix_n.device)
+        self.check(self.L.gtc_edge_count(self.h, _ptr(prefix_n), _ptr(parent), _ptr(edge), m, key_bits, _stream()))
+        return edge[:m]
+
+    def partial_sum(self, data, first: int, last: int, ws=None):
+        torch = _torch()
+        out = torch.zeros(max(last - first, 1), dtype=torch.int32, device=data.device)
+        self.check(self.L.gtc_partial_sum_u32(self.h, _ptr(data), first, last, _ptr(out), _ptr(ws),
+                                              0 if ws is None else ws.numel(), _stream()))
+        return out[: last - first]
+
+    def node_offsets(self, edge, n_brt_nodes: int, ws=None):
+        torch = _torch()
+        ps = torch.zeros(n_brt_nodes + 1, dtype=torch.int32, device=edge.device)
+        o = torch.zeros(1, dtype=torch.int32, device=edge.device)
+        self.check(self.L.gtc_node_offsets(self.h, _ptr(edge), n_brt_nodes, _ptr(ps), _ptr(o), _ptr(ws),
+                                           0 if ws is None else ws.numel(), _stream()))
+        return ps, o
+
+    def make_octree(self, codes, tree, edge, ps, n_oct: int, min_coord=0.0, rng=1024.0, link=True):
+        torch = _torch()
+        m = tree["prefix_n"].numel()
+        nodes = torch.zeros((max(n_oct, 1), 16), dtype=torch.int32, device=codes.device)
+        k64 = codes.element_size() == 8
+        mk = self.L.gtc_make_octree_u64 if k64 else self.L.gtc_make_octree_u32
+        self.check(mk(self.h, _ptr(nodes), max(n_oct, 1), _ptr(ps), _ptr(edge), _ptr(codes), _ptr(tree["prefix_n"]),
+                      _ptr(tree["parent"]), min_coord, rng, m, _ptr(tree["has_leaf_left"]),
+                      _ptr(tree["has_leaf_right"]), _ptr(tree["left_child"]), _stream()))
+        if link:
+            lk = self.L.gtc_link_octree_u64 if k64 else self.L.gtc_link_octree_u32
+            self.check(lk(self.h, _ptr(nodes), max(n_oct, 1), _ptr(ps), _ptr(edge), _ptr(codes),
+                          _ptr(tree["prefix_n"]), _ptr(tree["parent"]), m, _ptr(tree["has_leaf_left"]),
+                          _ptr(tree["has_leaf_right"]), _ptr(tree["left_child"]), _stream()))
+        return nodes[:n_oct]
+
+    # -- sort variant table (autotuner) ------------------------------------
+    def sort_variants(self):
+        out = []
+        for v in range(self.L.gtc_sort_num_variants()):
+            t, k = ctypes.c_int(), ctypes.c_int()
+            self.check(self.L.gtc_sort_variant_shape(v, ctypes.byref(t), ctypes.byref(k)))
+            out.append((t.value, k.value))
+        return out
+
+    def set_sort_variant(self, key_bits: int, v: int):
+        self.check(self.L.gtc_sort_set_variant(key_bits, v))
+
+    def get_sort_variant(self, key_bits: int) -> int:
+        return int(self.L.gtc_sort_get_variant(key_bits))
+
+
+@dataclass
+class OctreeResult:
+    keys: object
+    idx: object
+    prefix_n: object
+    has_leaf_left: object
+    has_leaf_right: object
+    left_child: object
+    parent: object
+    edge_count: object
+    node_offsets: object
+    nodes: object  # int32 [o, 16] view of gtc_octnode
+    n_unique: int
+    n_brt_nodes: int
+    n_oct_nodes: int
+
+
+class OctreePlan:
+    """Resident buffers for repeated builds of up to n_max points: the fused
+    stream-ordered pipeline (gtc_build_octree) with no allocation per call,
+    optionally captured once into a CUDA graph and replayed."""
+
+    def __init__(self, ctx: Context, n_max: int, key_bits: int, nodes_capacity: int | None = None):
+        torch = _torch()
+        self.ctx, self.n_max, self.key_bits = ctx, n_max, key_bits
+        dev = f"cuda:{ctx.device}"
+        n = max(n_max, 1)
+        kd = torch.int32 if key_bits == 32 else torch.int64
+        self.keys = torch.empty(n, dtype=kd, device=dev)
+        self.idx = torch.empty(n, dtype=torch.int32, device=dev)
+        self.prefix_n = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.hll = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.hlr = torch.empty(n, dtype=torch.uint8, device=dev)
+        self.left = torch.empty(n, dtype=torch.int32, device=dev)
+        self.parent = torch.empty(n, dtype=torch.int32, device=dev)
+        self.edge = torch.empty(n, dtype=torch.int32, device=dev)
+        self.ps = torch.empty(n, dtype=torch.int32, device=dev)
+        self.nodes_capacity = nodes_capacity or (n + 1024)
+        self.nodes = torch.empty((self.nodes_capacity, 16), dtype=torch.int32, device=dev)
+        self.counts = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.ws = ctx.workspace(OP_BUILD_OCTREE, n, key_bits)
+        self.bufs = OctreeBuffers(_ptr(self.keys), _ptr(self.idx), _ptr(self.prefix_n), _ptr(self.hll),
+                                  _ptr(self.hlr), _ptr(self.left), _ptr(self.parent), _ptr(self.edge),
+                                  _ptr(self.ps), _ptr(self.nodes), self.nodes_capacity, _ptr(self.counts))
+        self.graph = None
+
+    def launch(self, pts, n: int | None = None, min_coord=0.0, rng=1024.0, stream=None):
+        n = pts.shape[0] if n is None else n
+        assert n <= self.n_max
+        self.ctx.check(self.ctx.L.gtc_build_octree(self.ctx.h, _ptr(pts), n, min_coord, rng, self.key_bits,
+                                                   ctypes.byref(self.bufs), _ptr(self.ws), self.ws.numel(),
+                                                   _stream(stream)))
+
+    def capture(self, pts, n: int | None = None, min_coord=0.0, rng=1024.0):
+        """Capture the whole pipeline for `pts` into a CUDA graph."""
+        torch = _torch()
+        self.launch(pts, n, min_coord, rng)  # warm-up (sets kernel attributes)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            g.capture_begin()
+            self.launch(pts, n, min_coord, rng, stream=s)
+            g.capture_end()
+        torch.cuda.synchronize()
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def counts_host(self):
+        c = self.counts.cpu().numpy()
+        return int(c[0]), int(c[1]), int(c[2])
+
+    def result(self) -> OctreeResult:
+        u, m, o = self.counts_host()
+        self.ctx.device_status()
+        return OctreeResult(self.keys[:u], self.idx[:u], self.prefix_n[:m], self.hll[:m], self.hlr[:m],
+                            self.left[:m], self.parent[:m], self.edge[:m], self.ps[:u], self.nodes[:o], u, m, o)
+
+
+def build_octree(ctx: Context, pts, key_bits: int, min_coord=0.0, rng=1024.0) -> OctreeResult:
+    plan = OctreePlan(ctx, pts.shape[0], key_bits)
+    plan.launch(pts, min_coord=min_coord, rng=rng)
+    u, m, o = plan.counts_host()
+    if o > plan.nodes_capacity:
+        ctx.device_status_code()
+        plan = OctreePlan(ctx, pts.shape[0], key_bits, nodes_capacity=o)
+        plan.launch(pts, min_coord=min_coord, rng=rng)
+    return plan.result()
+
+
+def nodes_to_numpy(nodes) -> np.ndarray:
+    """int32 [o, 16] device/host tensor -> structured gtc_octnode array."""
+    a = nodes.cpu().numpy() if hasattr(nodes, "cpu") else np.asarray(nodes)
+    return np.ascontiguousarray(a).view(OCTNODE_DTYPE).reshape(-1)

@@ -1,0 +1,302 @@
+/*
+ * gtc.h - C ABI of the GB300-native point-cloud -> octree construction path.
+ *
+ * Drop-in boundary for the stage-by-stage operator surface of
+ * ucsc-redwood/glsl-tree-construction (vulkan/radixsort-vulkan/src/*.rs).
+ * Every entry point below names the reference operator it replaces.
+ *
+ * Two families of entry points:
+ *   1. Stream-ordered device entry points (gtc_*): device pointers, caller-owned
+ *      buffers, an explicit cudaStream_t, no host synchronisation.  Sizes that
+ *      depend on data (unique count, octree node count) stay on the device.
+ *   2. Host-buffer shims with the reference's own parameter order (gtc_ref_*):
+ *      synchronous, host arrays in and out, like the Rust functions they
+ *      replace.  `group_size` (the reference's workgroup count) is accepted and
+ *      ignored: launch shapes come from the tuned kernel table.
+ *
+ * Errors are returned as gtc_status; nothing aborts.  Device-side conditions
+ * (a bounded wait that ran out, a capacity overflow) are recorded in a status
+ * word that gtc_device_status() reads after synchronising.
+ *
+ * Key conventions: 32-bit Morton codes carry 10 bits per axis (30 bits used),
+ * 64-bit codes carry 21 bits per axis (63 bits used).  Points are float[n][4]
+ * (x, y, z, w), 16-byte stride, as in morton.comp:18-20.  All counts < 2^30.
+ */
+#ifndef GTC_H
+#define GTC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GTC_API __attribute__((visibility("default")))
+#else
+#define GTC_API
+#endif
+
+/* A cudaStream_t (0 = legacy default stream). */
+typedef void* gtc_stream_t;
+
+typedef enum gtc_status {
+  GTC_OK = 0,
+  GTC_ERR_INVALID_ARG = 1,
+  GTC_ERR_OOM = 2,
+  GTC_ERR_CUDA = 3,
+  GTC_ERR_TIMEOUT = 4,          /* a bounded device wait ran out */
+  GTC_OVERFLOW_FALLBACK = 5,    /* learned path rejected the input; onesweep produced the result */
+  GTC_ERR_UNSUPPORTED = 6,
+  GTC_ERR_CAPACITY = 7          /* an output buffer was too small (octree nodes) */
+} gtc_status;
+
+/* Octree node: the 64-byte std430 layout of octree.comp:14-20
+ * (children at 0, corner at 32, cell_size at 48, masks at 52/56). */
+typedef struct gtc_octnode {
+  int32_t children[8];
+  float corner[4];
+  float cell_size;
+  int32_t child_node_mask;
+  int32_t child_leaf_mask;
+  int32_t _pad;
+} gtc_octnode;
+
+typedef struct gtc_ctx gtc_ctx;
+
+/* ------------------------------------------------------------ context ---- */
+GTC_API gtc_status gtc_create(gtc_ctx** out, int device);
+GTC_API gtc_status gtc_destroy(gtc_ctx* ctx);
+GTC_API const char* gtc_status_string(gtc_status s);
+/* Text of the last error raised on this context (empty if none). */
+GTC_API const char* gtc_last_error(gtc_ctx* ctx);
+/* Synchronises `stream`, then returns and clears the device status word
+ * (GTC_ERR_TIMEOUT / GTC_ERR_CAPACITY, or GTC_OK). */
+GTC_API gtc_status gtc_device_status(gtc_ctx* ctx, gtc_stream_t stream);
+/* Library version string and the number of kernel variants compiled in. */
+GTC_API const char* gtc_version(void);
+
+/* Record per-stage CUDA events around every launch (0 = off, the default). */
+GTC_API gtc_status gtc_set_profiling(gtc_ctx* ctx, int enable);
+/* Sum of event-timed milliseconds per stage since the last reset, and the
+ * number of launches timed.  Stages: see GTC_STAGE_*.  Synchronises. */
+enum {
+  GTC_STAGE_MORTON = 0,
+  GTC_STAGE_HISTOGRAM = 1,
+  GTC_STAGE_ONESWEEP = 2,
+  GTC_STAGE_UNIQUE = 3,
+  GTC_STAGE_RADIX_TREE = 4,
+  GTC_STAGE_PREFIX_SUM = 5,
+  GTC_STAGE_OCTREE = 6,
+  GTC_STAGE_LEARNED = 7,
+  GTC_STAGE_COUNT = 8
+};
+GTC_API gtc_status gtc_stage_times(gtc_ctx* ctx, float* ms, uint32_t* launches, int reset);
+
+/* --------------------------------------------------------- workspace ----- */
+typedef enum gtc_op {
+  GTC_OP_SORT_PAIRS = 1,
+  GTC_OP_UNIQUE = 2,
+  GTC_OP_PARTIAL_SUM = 3,
+  GTC_OP_BUILD_OCTREE = 4,
+  GTC_OP_GLOBAL_HISTOGRAM = 5
+} gtc_op;
+/* Bytes of device workspace `op` needs for n elements of key_bits-wide keys.
+ * Workspace pointers must be 256-byte aligned. */
+GTC_API gtc_status gtc_workspace_size(gtc_ctx* ctx, gtc_op op, uint32_t n, int key_bits, size_t* bytes);
+
+/* ----------------------------------------------------- stage operators --- */
+
+/* Morton encode.  Replaces compute_morton (morton.rs:76-83, morton.comp:36-67):
+ * q = trunc(((x - min) / range) * 2^B), masked to B bits, bits interleaved
+ * x | y << 1 | z << 2.  idx (nullable) receives 0..n-1, the payload the sort
+ * carries. */
+GTC_API gtc_status gtc_morton32(gtc_ctx* ctx, const float* pts, uint32_t* keys, uint32_t* idx, uint32_t n,
+                                float min_coord, float range, gtc_stream_t stream);
+GTC_API gtc_status gtc_morton64(gtc_ctx* ctx, const float* pts, uint64_t* keys, uint32_t* idx, uint32_t n,
+                                float min_coord, float range, gtc_stream_t stream);
+
+/* Global digit histograms, written as exclusive prefixes per pass:
+ * hist[pass * 256 + digit], passes = ceil((end_bit - begin_bit) / 8).
+ * Replaces histogram (histogram.rs:38, histogram.comp:103-195), with correct
+ * counts (the shader masks one digit with 0xF at histogram.comp:128). */
+GTC_API gtc_status gtc_global_histogram_u32(gtc_ctx* ctx, const uint32_t* keys, uint32_t n, int begin_bit,
+                                            int end_bit, uint32_t* hist, void* ws, size_t ws_bytes,
+                                            gtc_stream_t stream);
+GTC_API gtc_status gtc_global_histogram_u64(gtc_ctx* ctx, const uint64_t* keys, uint32_t n, int begin_bit,
+                                            int end_bit, uint32_t* hist, void* ws, size_t ws_bytes,
+                                            gtc_stream_t stream);
+
+/* Stable LSD onesweep sort of (key, value) pairs on bits [begin_bit, end_bit).
+ * The result is in keys/vals; keys_alt/vals_alt are scratch of the same size.
+ * Replaces the onesweep driver test_radix_sort (main.rs:175-800,
+ * new_radix_sort.comp:116-314) and radix_sort (radixsort.rs:36).  vals may be
+ * NULL (keys only; vals_alt then ignored). */
+GTC_API gtc_status gtc_sort_pairs_u32(gtc_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t* keys_alt,
+                                      uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit, void* ws,
+                                      size_t ws_bytes, gtc_stream_t stream);
+GTC_API gtc_status gtc_sort_pairs_u64(gtc_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
+                                      uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit, void* ws,
+                                      size_t ws_bytes, gtc_stream_t stream);
+
+/* In-place unique of sorted keys: keeps the first of each run and its value;
+ * the count goes to *d_n_unique (device).  Replaces unique (unique.rs:37,
+ * unique.comp:31-49).  vals may be NULL. */
+GTC_API gtc_status gtc_unique_u32(gtc_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t n, uint32_t* d_n_unique,
+                                  void* ws, size_t ws_bytes, gtc_stream_t stream);
+GTC_API gtc_status gtc_unique_u64(gtc_ctx* ctx, uint64_t* keys, uint32_t* vals, uint32_t n, uint32_t* d_n_unique,
+                                  void* ws, size_t ws_bytes, gtc_stream_t stream);
+
+/* Karras radix tree over n_brt_nodes = u - 1 internal nodes (codes holds u
+ * sorted unique codes).  Replaces build_radix_tree (build_radix_tree.rs:34-43,
+ * build_radix_tree.comp:44-153) with a signed direction and a root range that
+ * covers all u keys.  edge_count (nullable) additionally receives the edge
+ * counts of edge_count.comp (fused). */
+GTC_API gtc_status gtc_build_radix_tree_u32(gtc_ctx* ctx, const uint32_t* codes, int32_t n_brt_nodes,
+                                            uint8_t* prefix_n, uint8_t* has_leaf_left, uint8_t* has_leaf_right,
+                                            int32_t* left_child, int32_t* parent, uint32_t* edge_count,
+                                            gtc_stream_t stream);
+GTC_API gtc_status gtc_build_radix_tree_u64(gtc_ctx* ctx, const uint64_t* codes, int32_t n_brt_nodes,
+                                            uint8_t* prefix_n, uint8_t* has_leaf_left, uint8_t* has_leaf_right,
+                                            int32_t* left_child, int32_t* parent, uint32_t* edge_count,
+                                            gtc_stream_t stream);
+
+/* edge[i] = depth(i) - depth(parent[i]), depth = (prefix_n - A) / 3 with
+ * A = key_bits - 3 * bits_per_axis.  Replaces edge_count (edge_count.rs:41-47,
+ * edge_count.comp:30-41) over exactly n_brt_nodes nodes. */
+GTC_API gtc_status gtc_edge_count(gtc_ctx* ctx, const uint8_t* prefix_n, const int32_t* parent,
+                                  uint32_t* edge_count, uint32_t n_brt_nodes, int key_bits, gtc_stream_t stream);
+
+/* Inclusive scan of data[first, last) into d_first[0, last - first).
+ * Replaces partial_sum (partial_sum.rs:43, partial_sum.comp:23-39). */
+GTC_API gtc_status gtc_partial_sum_u32(gtc_ctx* ctx, const uint32_t* data, uint32_t first, uint32_t last,
+                                       uint32_t* d_first, void* ws, size_t ws_bytes, gtc_stream_t stream);
+
+/* Octree node offsets as the pipeline uses them (main.rs:127-129): inclusive
+ * scan of edge_count over u = n_brt_nodes + 1 entries, edge[m] read as 0,
+ * node_offsets[0] = 0.  d_n_oct_nodes (nullable, device) receives
+ * o = 1 + node_offsets[u - 1]. */
+GTC_API gtc_status gtc_node_offsets(gtc_ctx* ctx, const uint32_t* edge_count, uint32_t n_brt_nodes,
+                                    uint32_t* node_offsets, uint32_t* d_n_oct_nodes, void* ws, size_t ws_bytes,
+                                    gtc_stream_t stream);
+
+/* Octree make: writes every octree node (root included, main.rs:140-153)
+ * with its internal children, corners and cell sizes.  Replaces build_octree /
+ * k_MakeOctNodes (octree.rs:73-87, octree.comp:126-186); same argument order.
+ * Radix node i owns slots [node_offsets[i] - rt_node_counts[i] + 1,
+ * node_offsets[i]]; the root owns slot 0.  oct_nodes must hold
+ * 1 + node_offsets[n_brt_nodes] nodes (nodes_capacity). */
+GTC_API gtc_status gtc_make_octree_u32(gtc_ctx* ctx, gtc_octnode* oct_nodes, uint32_t nodes_capacity,
+                                       const uint32_t* node_offsets, const uint32_t* rt_node_counts,
+                                       const uint32_t* codes, const uint8_t* rt_prefix_n, const int32_t* rt_parents,
+                                       float min_coord, float range, int32_t n_brt_nodes,
+                                       const uint8_t* rt_has_leaf_left, const uint8_t* rt_has_leaf_right,
+                                       const int32_t* rt_left_child, gtc_stream_t stream);
+GTC_API gtc_status gtc_make_octree_u64(gtc_ctx* ctx, gtc_octnode* oct_nodes, uint32_t nodes_capacity,
+                                       const uint32_t* node_offsets, const uint32_t* rt_node_counts,
+                                       const uint64_t* codes, const uint8_t* rt_prefix_n, const int32_t* rt_parents,
+                                       float min_coord, float range, int32_t n_brt_nodes,
+                                       const uint8_t* rt_has_leaf_left, const uint8_t* rt_has_leaf_right,
+                                       const int32_t* rt_left_child, gtc_stream_t stream);
+/* Octree link: adds the leaf children (k_LinkLeafNodes, octree.comp:188-222,
+ * commented out in the reference) after gtc_make_octree_*. */
+GTC_API gtc_status gtc_link_octree_u32(gtc_ctx* ctx, gtc_octnode* oct_nodes, uint32_t nodes_capacity,
+                                       const uint32_t* node_offsets, const uint32_t* rt_node_counts,
+                                       const uint32_t* codes, const uint8_t* rt_prefix_n, const int32_t* rt_parents,
+                                       int32_t n_brt_nodes, const uint8_t* rt_has_leaf_left,
+                                       const uint8_t* rt_has_leaf_right, const int32_t* rt_left_child,
+                                       gtc_stream_t stream);
+GTC_API gtc_status gtc_link_octree_u64(gtc_ctx* ctx, gtc_octnode* oct_nodes, uint32_t nodes_capacity,
+                                       const uint32_t* node_offsets, const uint32_t* rt_node_counts,
+                                       const uint64_t* codes, const uint8_t* rt_prefix_n, const int32_t* rt_parents,
+                                       int32_t n_brt_nodes, const uint8_t* rt_has_leaf_left,
+                                       const uint8_t* rt_has_leaf_right, const int32_t* rt_left_child,
+                                       gtc_stream_t stream);
+
+/* --------------------------------------------------- fused pipeline ------ */
+
+/* Caller-owned device outputs of the whole path, each sized for n points
+ * (n >= 1).  counts[0..3] (device) receives u, m = u - 1, o and a status. */
+typedef struct gtc_octree_buffers {
+  void* keys;              /* uint32_t or uint64_t [n]: sorted unique codes (first u) */
+  uint32_t* idx;           /* [n]: original point index of each unique code (first u) */
+  uint8_t* prefix_n;       /* [n]: first m */
+  uint8_t* has_leaf_left;  /* [n]: first m */
+  uint8_t* has_leaf_right; /* [n]: first m */
+  int32_t* left_child;     /* [n]: first m */
+  int32_t* parent;         /* [n]: first m */
+  uint32_t* edge_count;    /* [n]: first m */
+  uint32_t* node_offsets;  /* [n]: first u */
+  gtc_octnode* nodes;      /* [nodes_capacity]: first o */
+  uint32_t nodes_capacity;
+  uint32_t* counts;        /* [4] device */
+} gtc_octree_buffers;
+
+/* Points -> Morton -> onesweep sort -> unique -> radix tree (+ edge count)
+ * -> node offsets -> octree make+link, all stream-ordered with no host sync
+ * (the commented pipeline of main.rs:60-170, with the GPU sort in place of the
+ * CPU sort at main.rs:85).  key_bits = 32 or 64. */
+GTC_API gtc_status gtc_build_octree(gtc_ctx* ctx, const float* pts, uint32_t n, float min_coord, float range,
+                                    int key_bits, const gtc_octree_buffers* out, void* ws, size_t ws_bytes,
+                                    gtc_stream_t stream);
+
+/* The same from HOST buffers: copies pts in, builds on the context's own
+ * resident buffers, copies the o octree nodes out (host_nodes holds
+ * host_nodes_capacity nodes) and host_counts[0..2] = u, m, o.  Synchronous.
+ * Host buffers should be pinned (cudaHostAlloc) for full copy bandwidth. */
+GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, uint32_t n, float min_coord,
+                                         float range, int key_bits, gtc_octnode* host_nodes,
+                                         uint32_t host_nodes_capacity, uint32_t* host_counts);
+
+/* ------------------------------------------------------ sort variants --- */
+/* Onesweep tile shapes compiled into the library (threads per block and keys
+ * per thread); the autotuner times them and selects one per key width.  No
+ * reference counterpart: the reference hard-codes 512 x 15 (main.rs:182). */
+GTC_API int gtc_sort_num_variants(void);
+GTC_API gtc_status gtc_sort_variant_shape(int variant, int* threads, int* keys_per_thread);
+GTC_API gtc_status gtc_sort_set_variant(int key_bits, int variant);
+GTC_API int gtc_sort_get_variant(int key_bits);
+
+/* Pinned host memory helpers for callers without a CUDA runtime binding. */
+GTC_API gtc_status gtc_host_alloc(void** ptr, size_t bytes);
+GTC_API gtc_status gtc_host_free(void* ptr);
+
+/* ------------------------------------------- reference-signature shims --- */
+/* Synchronous host-array versions with the Rust functions' parameter order.
+ * They use a process-wide context on device 0. */
+
+/* morton.rs:76-83  compute_morton(input, morton_keys, n, min_coord, range, group_size) */
+GTC_API gtc_status gtc_ref_compute_morton(const float* input, uint32_t* morton_keys, uint32_t n, float min_coord,
+                                          float range, uint32_t group_size);
+/* morton.rs:43-60  morton32_to_xyz(ret, code, min_coord, range) */
+GTC_API void gtc_ref_morton32_to_xyz(float* ret, uint32_t code, float min_coord, float range);
+/* histogram.rs:38  histogram(input_size, input_data, global_hist[1024]) */
+GTC_API gtc_status gtc_ref_histogram(uint32_t input_size, const uint32_t* input_data, uint32_t* global_hist);
+/* radixsort.rs:36  radix_sort(in_data, n, out_data, group_size) (onesweep) */
+GTC_API gtc_status gtc_ref_radix_sort(const uint32_t* in_data, uint32_t n, uint32_t* out_data, uint32_t group_size);
+/* unique.rs:37  unique(u_sort, n) -> n_unique (in place) */
+GTC_API uint32_t gtc_ref_unique(uint32_t* u_sort, uint32_t n);
+/* build_radix_tree.rs:34-43 */
+GTC_API gtc_status gtc_ref_build_radix_tree(int32_t n, const uint32_t* codes, uint8_t* prefix_n,
+                                            uint8_t* has_leaf_left, uint8_t* has_leaf_right, int32_t* left_child,
+                                            int32_t* parent, uint32_t group_size);
+/* edge_count.rs:41-47 (n_brt_nodes is the number of radix-tree nodes, m) */
+GTC_API gtc_status gtc_ref_edge_count(const uint8_t* prefix_n, const int32_t* parent, uint32_t* u_edge_count,
+                                      uint32_t n_brt_nodes, uint32_t group_size);
+/* partial_sum.rs:43 */
+GTC_API gtc_status gtc_ref_partial_sum(const uint32_t* u_edge_count, uint32_t first, uint32_t last,
+                                       uint32_t* d_first);
+/* octree.rs:73-87 build_octree(...) followed by the link step; n = radix-tree
+ * node count m; oct_nodes holds 1 + node_offsets[m] nodes. */
+GTC_API gtc_status gtc_ref_build_octree(gtc_octnode* oct_nodes, const uint32_t* node_offsets,
+                                        const uint32_t* rt_node_counts, const uint32_t* codes,
+                                        const uint8_t* rt_prefix_n, const int32_t* rt_parents, float min_coord,
+                                        float range, int32_t n, const uint8_t* rt_has_leaf_left,
+                                        const uint8_t* rt_has_leaf_right, const int32_t* rt_left_child,
+                                        uint32_t group_size);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GTC_H */

@@ -1,0 +1,67 @@
+"""The C-ABI library loads and exports every entry point include/gtc.h
+declares; host-side argument checking works without a GPU."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "gtc.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"GTC_API\s+[\w\s\*]+?\b(gtc_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_stage_surface():
+    syms = declared_symbols()
+    for s in ("gtc_morton32", "gtc_morton64", "gtc_global_histogram_u32", "gtc_sort_pairs_u32", "gtc_sort_pairs_u64",
+              "gtc_unique_u32", "gtc_build_radix_tree_u32", "gtc_edge_count", "gtc_partial_sum_u32",
+              "gtc_make_octree_u32", "gtc_link_octree_u32", "gtc_build_octree", "gtc_build_octree_host",
+              "gtc_ref_compute_morton", "gtc_ref_build_octree"):
+        assert s in syms, s
+
+
+def test_library_exports_every_declared_symbol(gtc_mod):
+    L = gtc_mod.lib()
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", gtc_mod._lib.lib_path()], capture_output=True, text=True)
+    exported = set(re.findall(r"\b(gtc_\w+)$", out.stdout, re.M))
+    assert set(declared_symbols()) <= exported
+
+
+def test_status_strings_and_version(gtc_mod):
+    L = gtc_mod.lib()
+    assert L.gtc_status_string(0) == b"ok"
+    assert L.gtc_status_string(4).startswith(b"a bounded")
+    assert b"sm_103a" in L.gtc_version()
+
+
+def test_workspace_size_without_device(gtc_mod):
+    L = gtc_mod.lib()
+    b = ctypes.c_size_t()
+    assert L.gtc_workspace_size(None, gtc_mod.OP_SORT_PAIRS, 10_000_000, 64, ctypes.byref(b)) == 0
+    tiles = -(-10_000_000 // 4096)
+    assert b.value >= 8 * tiles * 256 * 4
+    assert L.gtc_workspace_size(None, gtc_mod.OP_BUILD_OCTREE, 1 << 20, 32, ctypes.byref(b)) == 0
+    assert b.value >= (1 << 20) * 8
+    assert L.gtc_workspace_size(None, gtc_mod.OP_SORT_PAIRS, 100, 48, ctypes.byref(b)) == 1  # bad key width
+
+
+def test_null_context_is_rejected(gtc_mod):
+    L = gtc_mod.lib()
+    assert L.gtc_morton32(None, None, None, None, 0, 0.0, 1.0, None) == 1
+    assert L.gtc_sort_pairs_u32(None, None, None, None, None, 10, 0, 32, None, 0, None) == 1
+
+
+@pytest.mark.skipif(os.environ.get("CUDA_VISIBLE_DEVICES", None) == "" or
+                    __import__("torch").cuda.is_available(), reason="checks the no-device path")
+def test_create_without_device_fails_cleanly(gtc_mod):
+    L = gtc_mod.lib()
+    h = ctypes.c_void_p()
+    assert L.gtc_create(ctypes.byref(h), 0) == 3  # GTC_ERR_CUDA, no abort
+    assert not h.value

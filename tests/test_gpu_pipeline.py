@@ -1,0 +1,117 @@
+"""End-to-end parity of the fused pipeline (gtc_build_octree) with the oracle:
+every stage buffer and every octree node, byte for byte."""
+import numpy as np
+import pytest
+
+from gtc import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _cmp(res, exp, key_bits, tag=""):
+    import gtc
+
+    kd = np.uint32 if key_bits == 32 else np.uint64
+    assert (res.n_unique, res.n_brt_nodes, res.n_oct_nodes) == (exp["n_unique"], exp["n_brt_nodes"],
+                                                                 exp["n_oct_nodes"]), tag
+    pairs = [("keys", res.keys, kd), ("idx", res.idx, np.uint32), ("prefix_n", res.prefix_n, np.uint8),
+             ("has_leaf_left", res.has_leaf_left, np.uint8), ("has_leaf_right", res.has_leaf_right, np.uint8),
+             ("left_child", res.left_child, np.int32), ("parent", res.parent, np.int32),
+             ("edge_count", res.edge_count, np.uint32), ("node_offsets", res.node_offsets, np.uint32)]
+    for name, t, dt in pairs:
+        got = t.cpu().numpy().view(dt)
+        assert np.array_equal(got, exp[name]), (tag, name)
+    got_nodes = gtc.nodes_to_numpy(res.nodes)
+    assert np.array_equal(got_nodes.view(np.int32), exp["nodes"].view(np.int32)), (tag, "nodes")
+
+
+def _run(ctx, oracle, pts, key_bits, tag):
+    import gtc
+    import torch
+
+    res = gtc.build_octree(ctx, torch.from_numpy(pts).cuda(), key_bits)
+    exp, _ = oracle.build_octree(pts, key_bits, threads=8)
+    assert exp["conflicts"] == 0
+    _cmp(res, exp, key_bits, tag)
+    assert oracle.validate_octree(gtc.nodes_to_numpy(res.nodes), res.n_unique) == 0
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
+def test_config1_uniform_2p20(ctx, oracle, key_bits):
+    _run(ctx, oracle, W.config1_points(), key_bits, "config1")
+
+
+def test_config2_clustered_10m(ctx, oracle):
+    _run(ctx, oracle, W.config2_points(), 64, "config2")
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
+def test_edge_cases(ctx, oracle, key_bits):
+    def p(xyz):
+        xyz = np.asarray(xyz, np.float32).reshape(-1, 3)
+        out = np.ones((xyz.shape[0], 4), np.float32)
+        out[:, :3] = xyz
+        return out
+
+    cases = {
+        "n1": p([[1.0, 2.0, 3.0]]),
+        "n2": p([[1.0, 2.0, 3.0], [700.0, 2.0, 3.0]]),
+        "all_equal": p([[5.5, 6.5, 7.5]] * 5000),
+        "corners": p([[x, y, z] for z in (10.0, 600.0) for y in (10.0, 600.0) for x in (10.0, 600.0)]),
+        "boundary": p([[1024.0, 0.0, 0.0], [0.0, 1023.99, 0.0], [0.0, 0.0, 0.0], [512.0, 512.0, 512.0]]),
+        "duplicates": np.repeat(W.uniform_points(3000, seed=4), 7, axis=0),
+        "line": p([[float(i) * 0.25, 1.0, 1.0] for i in range(4096)]),
+        "ragged": W.uniform_points(123_457, seed=8),
+        "dense_cluster": W.gaussian_mixture_points(200_000, 1, 0.05, seed=6),
+    }
+    for tag, pts in cases.items():
+        _run(ctx, oracle, np.ascontiguousarray(pts), key_bits, tag)
+
+
+def test_empty_input(ctx):
+    import gtc
+    import torch
+
+    plan = gtc.OctreePlan(ctx, 16, 32)
+    plan.launch(torch.zeros((0, 4), dtype=torch.float32, device="cuda"), n=0)
+    assert plan.counts_host() == (0, 0, 0)
+
+
+def test_graph_replay_matches_direct(ctx, oracle):
+    import gtc
+    import torch
+
+    pts = W.gaussian_mixture_points(500_000, 8, 10.0, noise=0.05, seed=12)
+    tp = torch.from_numpy(pts).cuda()
+    plan = gtc.OctreePlan(ctx, pts.shape[0], 64)
+    plan.capture(tp)
+    for _ in range(3):
+        plan.replay()
+    torch.cuda.synchronize()
+    exp, _ = oracle.build_octree(pts, 64, threads=8)
+    _cmp(plan.result(), exp, 64, "graph")
+
+
+def test_host_buffer_entry_point(ctx, oracle):
+    import ctypes
+
+    pts = W.config1_points(1 << 18)
+    exp, _ = oracle.build_octree(pts, 32)
+    nodes = np.zeros(exp["n_oct_nodes"] + 16, oracle.OCTNODE_DTYPE)
+    counts = np.zeros(3, np.uint32)
+    s = ctx.L.gtc_build_octree_host(ctx.h, pts.ctypes.data_as(ctypes.c_void_p), pts.shape[0], 0.0, 1024.0, 32,
+                                    nodes.ctypes.data_as(ctypes.c_void_p), nodes.size,
+                                    counts.ctypes.data_as(ctypes.c_void_p))
+    ctx.check(s)
+    assert tuple(counts) == (exp["n_unique"], exp["n_brt_nodes"], exp["n_oct_nodes"])
+    assert np.array_equal(nodes[: counts[2]].view(np.int32), exp["nodes"].view(np.int32))
+
+
+def test_deterministic_across_runs(ctx):
+    import gtc
+    import torch
+
+    pts = torch.from_numpy(W.config2_points(2_000_000, seed=5)).cuda()
+    a = gtc.build_octree(ctx, pts, 64)
+    b = gtc.build_octree(ctx, pts, 64)
+    assert torch.equal(a.nodes, b.nodes) and torch.equal(a.keys, b.keys) and torch.equal(a.idx, b.idx)
