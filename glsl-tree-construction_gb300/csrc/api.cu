@@ -371,6 +371,12 @@ gtc_status ensure_resident(gtc_ctx* ctx, uint32_t n, int key_bits, uint32_t node
 
 }  // namespace
 
+namespace gtc {
+// Accessors for entry points defined in other translation units.
+Launch context_launch(gtc_ctx* ctx, gtc_stream_t stream) { return launch_of(ctx, stream); }
+gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_t e) { return fail(ctx, s, msg, e); }
+}  // namespace gtc
+
 // =================================================================== C ABI ==
 extern "C" {
 

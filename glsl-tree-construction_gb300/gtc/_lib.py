@@ -55,6 +55,7 @@ SIGNATURES = {
     "gtc_build_octree_host": (st, [P, P, u32, f32, f32, i_, P, u32, P]),
     "gtc_host_alloc": (st, [ctypes.POINTER(P), sz]),
     "gtc_host_free": (st, [P]),
+    "gtc_sort_pairs_u32_noalloc": (st, [P, P, P, P, P, u32, i_, i_, P]),
     "gtc_sort_num_variants": (i_, []),
     "gtc_sort_variant_shape": (st, [i_, ctypes.POINTER(i_), ctypes.POINTER(i_)]),
     "gtc_sort_set_variant": (st, [i_, i_]),

@@ -249,6 +249,23 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
                                          float range, int key_bits, gtc_octnode* host_nodes,
                                          uint32_t host_nodes_capacity, uint32_t* host_counts);
 
+/* The same sort of 32-bit keys (optionally with u32 values) for callers that
+ * must not allocate device memory at the point where they sort: cudaMalloc /
+ * cudaFree synchronise the device and can stall other streams for
+ * milliseconds, and callers whose own allocator owns the device memory cannot
+ * hand over a workspace on demand.  No counterpart in the reference.
+ * Its scratch is a fixed 4,210,944-byte array inside the library, held by
+ * every GPU that loads the library until the process exits, so n is limited
+ * to GTC_NOALLOC_MAX_KEYS (larger n returns GTC_ERR_INVALID_ARG).  The call
+ * allocates nothing.  Its first call on a device looks up that device's
+ * address of the array (once per device, with the device current); make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so issue them on one stream. */
+#define GTC_NOALLOC_MAX_KEYS 4194304u
+GTC_API gtc_status gtc_sort_pairs_u32_noalloc(gtc_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t* keys_alt,
+                                              uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
+                                              gtc_stream_t stream);
+
 /* ------------------------------------------------------ sort variants --- */
 /* Onesweep tile shapes compiled into the library (threads per block and keys
  * per thread); the autotuner times them and selects one per key width.  No
