@@ -41,11 +41,16 @@ FALLBACK_HBM_GBS = 6800.0
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["gtc", "reference"], default="gtc")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (default: the 10M workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["octree", "sort"], default="octree",
+                    help="octree: the 10M clustered full build (default); sort: onesweep pairs sort only")
+    ap.add_argument("--key-bits", type=int, default=64, help="sort workload: 32 or 64")
+    ap.add_argument("--and-words", type=int, default=0, help="sort workload: AND of k uniform words (0 = uniform)")
+    ap.add_argument("--sort-variant", type=int, default=None, help="force a compiled onesweep variant")
     return ap.parse_args()
 
 
@@ -82,6 +87,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # nvidia-smi needs a moment before its first sample
         except Exception:
             self.proc = None
         return self
@@ -341,10 +347,86 @@ def cpu_baseline(pts_np):
             "sample": f"{reps} full builds of the same {n}-point cloud with the oracle ({threads} threads)"}
 
 
+def run_gtc_sort(args):
+    """Sort-only workload: stable onesweep sort of (key, u32 index) pairs."""
+    import numpy as np
+    import torch
+
+    import gtc
+    from gtc import workloads as W
+
+    kb, n = args.key_bits, args.n
+    keys_np = W.config3_keys(n, kb, and_words=args.and_words, seed=1)
+    kd = np.int32 if kb == 32 else np.int64
+    src_k = torch.from_numpy(keys_np.view(kd)).cuda()
+    src_v = torch.arange(n, dtype=torch.int32, device="cuda")
+    ctx = gtc.Context(0)
+    if args.sort_variant is not None:
+        ctx.set_sort_variant(kb, args.sort_variant)
+    ws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
+    k, v = torch.empty_like(src_k), torch.empty_like(src_v)
+    ka, va = torch.empty_like(src_k), torch.empty_like(src_v)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        ctx.sort_pairs(k, v, 0, kb, ws=ws, keys_alt=ka, vals_alt=va)
+
+    for _ in range(max(args.warmup, 3)):
+        k.copy_(src_k)
+        v.copy_(src_v)
+        step()
+    torch.cuda.synchronize()
+    ctx.device_status()
+    ctx.set_profiling(True)
+    ctx.stage_times(reset=True)
+    total = 0.0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            k.copy_(src_k)  # restore the unsorted input outside the timed span
+            v.copy_(src_v)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+    stages = ctx.stage_times(reset=True)
+    ctx.device_status()
+    # correctness of the last step: sorted, and the values are a stable permutation
+    kk = k.cpu().numpy().view(np.uint32 if kb == 32 else np.uint64)
+    vv = v.cpu().numpy().view(np.uint32)
+    ok = bool(np.all(kk[1:] >= kk[:-1])) and bool(np.array_equal(keys_np[vv], kk))
+    ms = total / args.steps
+    passes = kb // 8
+    os_ms, os_n = stages["onesweep"]
+    avg = os_ms / max(os_n, 1)
+    K = kb // 8
+    pass_bytes = 2 * (K + 4) * n
+    peak, peak_kind = measured_hbm_peak()
+    line = {
+        "metric": "Mkeys/s sort", "value": round(n / (ms * 1e-3) / 1e6, 2), "unit": "Mkeys/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
+        "config": {"workload": f"sort_pairs_u{kb}_n{n}_and{args.and_words}", "passes": passes,
+                   "sort_variant": ctx.get_sort_variant(kb), "variants": ctx.sort_variants(), "sorted_ok": ok,
+                   "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
+                   "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4)},
+        "roofline": {"bound": "hbm", "kernel": "onesweep pass", "achieved": round(pass_bytes / (avg * 1e-3) / 1e9, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
+                     "traffic": None, "peak_kind": peak_kind, "avg_launch_ms": round(avg, 5)},
+        "gpu_launches": (1 + passes) * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sort":
+        run_gtc_sort(args)
     else:
         run_gtc(args)
 

@@ -25,16 +25,8 @@
 
 namespace gtc {
 
-template <class K>
-__device__ __forceinline__ void store_node(gtc_octnode* nodes, uint32_t slot, const int32_t ch[8], float4 corner,
-                                           float cell, int32_t nmask, int32_t lmask) {
-  int4* p = reinterpret_cast<int4*>(nodes + slot);
-  p[0] = make_int4(ch[0], ch[1], ch[2], ch[3]);
-  p[1] = make_int4(ch[4], ch[5], ch[6], ch[7]);
-  p[2] = make_int4(__float_as_int(corner.x), __float_as_int(corner.y), __float_as_int(corner.z),
-                   __float_as_int(corner.w));
-  p[3] = make_int4(__float_as_int(cell), nmask, lmask, 0);
-}
+constexpr int OCT_THREADS = 256;
+constexpr int OCT_CAP = 512;  // nodes staged per block pass (32 KB of shared memory)
 
 template <class K>
 __device__ __forceinline__ K level_prefix(K code, int level) {  // top 3*level bits, kept in place
@@ -49,17 +41,81 @@ __device__ __forceinline__ int child_slot(K code, int level) {  // octant at `le
   return (int)((code >> (3 * B - 3 * level)) & 7);
 }
 
+// children[w] = v with w known only at run time, kept in registers.
+__device__ __forceinline__ void set_child(int4& lo, int4& hi, int w, int32_t v) {
+  lo.x = (w == 0) ? v : lo.x;
+  lo.y = (w == 1) ? v : lo.y;
+  lo.z = (w == 2) ? v : lo.z;
+  lo.w = (w == 3) ? v : lo.w;
+  hi.x = (w == 4) ? v : hi.x;
+  hi.y = (w == 5) ? v : hi.y;
+  hi.z = (w == 6) ? v : hi.z;
+  hi.w = (w == 7) ? v : hi.w;
+}
+
+// Writes one 64-byte node, into the block's staging area or straight to HBM.
+struct NodeSink {
+  int4* stage;
+  gtc_octnode* nodes;
+  uint32_t first;
+  bool staged;
+  __device__ __forceinline__ void put(uint32_t slot, int4 a, int4 b, int4 c, int4 d) const {
+    int4* p = staged ? stage + (size_t)(slot - first) * 4 : reinterpret_cast<int4*>(nodes + slot);
+    p[0] = a;
+    p[1] = b;
+    p[2] = c;
+    p[3] = d;
+  }
+};
+
+// Children of the bottom octree node of radix node k: descend from q through
+// internal children of the same depth (edge == 0); a depth band holds at
+// most three prefix lengths, so LEVEL never exceeds 2 on valid input.
+template <class K, bool WITH_LEAVES, int LEVEL>
+__device__ __forceinline__ void gather(uint32_t q, int level, const K* __restrict__ codes,
+                                       const uint8_t* __restrict__ hll, const uint8_t* __restrict__ hlr,
+                                       const int32_t* __restrict__ left, const uint32_t* __restrict__ edge,
+                                       const uint32_t* __restrict__ ps, int4& lo, int4& hi, int32_t& nmask,
+                                       int32_t& lmask, uint32_t* status) {
+  const int32_t lc = left[q];
+  const bool leaf_side[2] = {hll[q] != 0, hlr[q] != 0};
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const uint32_t x = (uint32_t)(lc + side);
+    if (leaf_side[side]) {
+      if (WITH_LEAVES) {
+        const int w = child_slot<K>(codes[x], level);
+        set_child(lo, hi, w, (int32_t)x);
+        lmask |= 1 << w;
+      }
+    } else {
+      const uint32_t e = edge[x];
+      if (e > 0) {
+        const int w = child_slot<K>(codes[x], level);
+        set_child(lo, hi, w, (int32_t)ps[x]);
+        nmask |= 1 << w;
+      } else if (LEVEL < 2) {
+        gather<K, WITH_LEAVES, (LEVEL < 2 ? LEVEL + 1 : 2)>(x, level, codes, hll, hlr, left, edge, ps, lo, hi, nmask,
+                                                            lmask, status);
+      } else {
+        atomicOr(status, DEV_INTERNAL);
+      }
+    }
+  }
+}
+
 template <class K, bool WITH_LEAVES>
-__global__ void __launch_bounds__(256) octree_make_kernel(const K* __restrict__ codes, const uint32_t* d_u,
-                                                          uint32_t u_host, const uint8_t* __restrict__ prefix_n,
-                                                          const uint8_t* __restrict__ hll,
-                                                          const uint8_t* __restrict__ hlr,
-                                                          const int32_t* __restrict__ left,
-                                                          const uint32_t* __restrict__ edge,
-                                                          const uint32_t* __restrict__ ps, float mn, float rg,
-                                                          gtc_octnode* __restrict__ nodes, uint32_t capacity,
-                                                          uint32_t* status) {
+__global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __restrict__ codes, const uint32_t* d_u,
+                                                                  uint32_t u_host, const uint8_t* __restrict__ prefix_n,
+                                                                  const uint8_t* __restrict__ hll,
+                                                                  const uint8_t* __restrict__ hlr,
+                                                                  const int32_t* __restrict__ left,
+                                                                  const uint32_t* __restrict__ edge,
+                                                                  const uint32_t* __restrict__ ps, float mn, float rg,
+                                                                  gtc_octnode* __restrict__ nodes, uint32_t capacity,
+                                                                  uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
+  __shared__ int4 s_stage[OCT_CAP * 4];
   const uint32_t u = d_u ? *d_u : u_host;
   if (u == 0) return;
   const uint32_t m = u - 1;
@@ -69,68 +125,65 @@ __global__ void __launch_bounds__(256) octree_make_kernel(const K* __restrict__ 
         atomicOr(status, DEV_CAPACITY);
         return;
       }
-      const int32_t none[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      store_node<K>(nodes, 0, none, decode_corner<K>((K)0, mn, rg), rg, 0, 0);
+      const float4 c = decode_corner<K>((K)0, mn, rg);
+      NodeSink sink{nullptr, nodes, 0, false};
+      sink.put(0, make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0),
+               make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), __float_as_int(c.w)),
+               make_int4(__float_as_int(rg), 0, 0, 0));
     }
     return;
   }
   const int root_level = (prefix_n[0] - A) / 3;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += stride) {
-    const uint32_t c = edge[k];
-    if (c == 0 && k != 0) continue;
-    const K code_k = codes[k];
-    const int dk = (prefix_n[k] - A) / 3;
-    const uint32_t top = ps[k];
-    const uint32_t bottom = (k == 0) ? 0u : top - c + 1;
-    if (k != 0 && c > top) {  // slot 0 is the root's: inconsistent offsets
-      atomicOr(status, DEV_INTERNAL);
-      continue;
-    }
-    if ((k == 0 ? 1u : top + 1) > capacity) {
-      atomicOr(status, DEV_CAPACITY);
-      continue;
-    }
-    // Bottom node: gather children through same-depth descendants.
-    int32_t ch[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int32_t nmask = 0, lmask = 0;
-    uint32_t stack[4];
-    int sp = 0;
-    stack[sp++] = k;
-    while (sp > 0) {
-      const uint32_t q = stack[--sp];
-      const int32_t lc = left[q];
-#pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        const uint32_t x = (uint32_t)(lc + side);
-        const bool leaf = side ? hlr[q] : hll[q];
-        if (leaf) {
-          if (WITH_LEAVES) {
-            const int w = child_slot<K>(codes[x], dk + 1);
-            ch[w] = (int32_t)x;
-            lmask |= 1 << w;
-          }
-        } else if (edge[x] > 0) {
-          const int w = child_slot<K>(codes[x], dk + 1);
-          ch[w] = (int32_t)ps[x];
-          nmask |= 1 << w;
-        } else if (sp < 4) {
-          stack[sp++] = x;
-        } else {
+  for (uint32_t kb = blockIdx.x * OCT_THREADS; kb < m; kb += gridDim.x * OCT_THREADS) {
+    // Radix nodes [kb, kend) own the contiguous slots [first, last1).
+    const uint32_t kend = min(kb + (uint32_t)OCT_THREADS, m);
+    const uint32_t first = (kb == 0) ? 0u : ps[kb - 1] + 1;
+    const uint32_t last1 = ps[kend - 1] + 1;
+    const bool staged = last1 >= first && last1 - first <= (uint32_t)OCT_CAP && last1 <= capacity;
+    const NodeSink sink{s_stage, nodes, first, staged};
+    __syncthreads();  // the previous pass's flush has read the staging area
+    const uint32_t k = kb + threadIdx.x;
+    if (k < m) {
+      const uint32_t c = edge[k];
+      const uint32_t top = ps[k];
+      if (k == 0 || c > 0) {
+        if (k != 0 && c > top) {  // slot 0 is the root's: inconsistent offsets
           atomicOr(status, DEV_INTERNAL);
+        } else if (!staged && (k == 0 ? 1u : top + 1) > capacity) {
+          atomicOr(status, DEV_CAPACITY);
+        } else {
+          const uint32_t bottom = (k == 0) ? 0u : top - c + 1;
+          const K code_k = codes[k];
+          const int dk = (prefix_n[k] - A) / 3;
+          int4 lo = make_int4(0, 0, 0, 0), hi = make_int4(0, 0, 0, 0);
+          int32_t nmask = 0, lmask = 0;
+          gather<K, WITH_LEAVES, 0>(k, dk + 1, codes, hll, hlr, left, edge, ps, lo, hi, nmask, lmask, status);
+          float4 cr = decode_corner<K>(level_prefix<K>(code_k, dk), mn, rg);
+          float cell = __fdiv_rn(rg, (float)(1u << (dk - root_level)));
+          sink.put(bottom, lo, hi,
+                   make_int4(__float_as_int(cr.x), __float_as_int(cr.y), __float_as_int(cr.z), __float_as_int(cr.w)),
+                   make_int4(__float_as_int(cell), nmask, lmask, 0));
+          // Chain nodes above the bottom (levels dk - 1 .. dk - c + 1).
+          for (uint32_t j = 1; j < c; ++j) {
+            const int level = dk - (int)j;
+            int4 a = make_int4(0, 0, 0, 0), b = make_int4(0, 0, 0, 0);
+            const int w = child_slot<K>(code_k, level + 1);
+            set_child(a, b, w, (int32_t)(bottom + j - 1));
+            cr = decode_corner<K>(level_prefix<K>(code_k, level), mn, rg);
+            cell = __fdiv_rn(rg, (float)(1u << (level - root_level)));
+            sink.put(bottom + j, a, b,
+                     make_int4(__float_as_int(cr.x), __float_as_int(cr.y), __float_as_int(cr.z),
+                               __float_as_int(cr.w)),
+                     make_int4(__float_as_int(cell), 1 << w, 0, 0));
+          }
         }
       }
     }
-    store_node<K>(nodes, bottom, ch, decode_corner<K>(level_prefix<K>(code_k, dk), mn, rg),
-                  __fdiv_rn(rg, (float)(1u << (dk - root_level))), nmask, lmask);
-    // Chain nodes above the bottom (levels dk - 1 .. dk - c + 1).
-    for (uint32_t j = 1; j < c; ++j) {
-      const int level = dk - (int)j;
-      int32_t one[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      const int w = child_slot<K>(code_k, level + 1);
-      one[w] = (int32_t)(bottom + j - 1);
-      store_node<K>(nodes, bottom + j, one, decode_corner<K>(level_prefix<K>(code_k, level), mn, rg),
-                    __fdiv_rn(rg, (float)(1u << (level - root_level))), 1 << w, 0);
+    __syncthreads();
+    if (staged) {  // coalesced 16-byte stores of the block's contiguous node range
+      int4* dst = reinterpret_cast<int4*>(nodes + first);
+      const uint32_t words = (last1 - first) * 4;
+      for (uint32_t x = threadIdx.x; x < words; x += OCT_THREADS) dst[x] = s_stage[x];
     }
   }
 }
@@ -142,12 +195,12 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
                                gtc_octnode* nodes, uint32_t capacity, bool with_leaves) {
   const uint32_t work = d_u ? n_max : u_host;
   if (work == 0) return cudaSuccess;
-  const uint32_t grid = max(1u, min(ceil_div(work, 256), (uint32_t)L.num_sms * 8));
+  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 6));
   if (with_leaves)
-    octree_make_kernel<K, true><<<grid, 256, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left, edge, ps,
+    octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left, edge, ps,
                                                              mn, rg, nodes, capacity, L.status);
   else
-    octree_make_kernel<K, false><<<grid, 256, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left, edge, ps,
+    octree_make_kernel<K, false><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left, edge, ps,
                                                               mn, rg, nodes, capacity, L.status);
   return cudaGetLastError();
 }

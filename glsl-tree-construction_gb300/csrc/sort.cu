@@ -270,16 +270,222 @@ __global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__
   }
 }
 
+// ------------------------------------------- persistent TMA onesweep ------
+// The same pass as onesweep_kernel, restructured so HBM never idles:
+//   * persistent CTAs (a few per SM) pull tile tickets in a loop;
+//   * each CTA double-buffers tiles in shared memory: while it ranks and
+//     scatters tile t, a TMA bulk copy (cp.async.bulk + mbarrier) is already
+//     streaming the keys and values of its next tile into the other buffer;
+//   * ranking: early per-warp digit counts (one shared atomic per peer group
+//     from __match_any_sync or 8 ballots), block offsets, then per key a
+//     leader atomicAdd on the warp's digit cursor returns the rank base, so
+//     consecutive keys carry no register dependency on each other;
+//   * the tile aggregate is published before ranking and the look-back is
+//     done after the tile is already scattered in shared memory, so
+//     predecessors have had the longest time to publish inclusive prefixes.
+// Forward progress: a CTA owns at most a current and a prefetched ticket and
+// processes its tickets in increasing order; the lowest unfinished tile is
+// always some CTA's current tile and only waits on finished tiles.
+template <class K, int THREADS, int KPT, bool HV>
+struct TmaSmem {
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int TILE = THREADS * KPT;
+  K keys[2][TILE];
+  uint32_t vals[2][HV ? TILE : 4];
+  uint32_t cnt[WARPS][RADIX];
+  uint32_t digit_off[RADIX];
+  uint32_t gbase[RADIX];
+  uint32_t warp_sums[8];
+  uint32_t next_tile;
+  uint32_t pending;
+  uint64_t bar[2];
+};
+
+template <bool MATCH>
+__device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
+  if (MATCH) return __match_any_sync(0xffffffffu, d);
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const uint32_t bit = (d >> b) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bal : ~bal;
+  }
+  return peers;
+}
+
+template <class K, int THREADS, int KPT, bool HV, bool MATCH>
+__global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tma_kernel(const K* __restrict__ kin,
+                                                               const uint32_t* __restrict__ vin, K* __restrict__ kout,
+                                                               uint32_t* __restrict__ vout, uint32_t n, int shift,
+                                                               uint32_t dmask, const uint32_t* __restrict__ bin_off,
+                                                               uint32_t* __restrict__ desc,
+                                                               uint32_t* __restrict__ tile_counter,
+                                                               uint32_t* __restrict__ status) {
+  using S = TmaSmem<K, THREADS, KPT, HV>;
+  constexpr int TILE = S::TILE;
+  constexpr int WARPS = S::WARPS;
+  static_assert(THREADS >= RADIX, "one thread per digit");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S& s = *reinterpret_cast<S*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t tiles = (n + TILE - 1) / TILE;
+  const uint32_t full_tiles = n / TILE;  // complete tiles come by TMA, a ragged last tile by plain loads
+
+  auto issue = [&](uint32_t t, int b) {  // thread 0 only
+    constexpr uint32_t kb = TILE * sizeof(K);
+    constexpr uint32_t vb = TILE * 4;
+    mbar_arrive_expect_tx(&s.bar[b], kb + (HV ? vb : 0u));
+    tma_load_1d(s.keys[b], kin + (size_t)t * TILE, kb, &s.bar[b]);
+    if (HV) tma_load_1d(s.vals[b], vin + (size_t)t * TILE, vb, &s.bar[b]);
+    s.pending |= 1u << b;
+  };
+
+  for (int i = tid; i < WARPS * RADIX; i += THREADS) (&s.cnt[0][0])[i] = 0;
+  if (tid == 0) {
+    mbar_init(&s.bar[0], 1);
+    mbar_init(&s.bar[1], 1);
+    fence_mbar_init();
+    s.pending = 0;
+    const uint32_t t = atomicAdd(tile_counter, 1u);
+    s.next_tile = t;
+    if (t < full_tiles) issue(t, 0);
+  }
+  __syncthreads();
+  uint32_t tile = s.next_tile;
+  int buf = 0;
+  uint32_t parity = 0;  // bit b: phase parity to wait for on buffer b
+
+  while (tile < tiles) {
+    __syncthreads();  // every thread has read s.next_tile
+    if (tid == 0) {
+      const uint32_t nt = atomicAdd(tile_counter, 1u);
+      s.next_tile = nt;
+      if (nt < full_tiles) issue(nt, buf ^ 1);
+    }
+    const uint32_t base = tile * TILE;
+    const uint32_t valid = min((uint32_t)TILE, n - base);
+    if (tile < full_tiles) {
+      bool ok = mbar_wait_bounded(&s.bar[buf], (parity >> buf) & 1u, status);
+      if (__syncthreads_or(!ok)) {
+        // A copy that never landed: wait (bounded) for anything still in
+        // flight into this CTA's shared memory, then leave; the successors'
+        // bounded look-backs report the timeout.
+        if (tid == 0) {
+          for (int b = 0; b < 2; ++b)
+            if (s.pending & (1u << b)) mbar_wait_bounded(&s.bar[b], (parity >> b) & 1u, status);
+        }
+        __syncthreads();
+        return;
+      }
+      parity ^= 1u << buf;
+      if (tid == 0) s.pending &= ~(1u << buf);
+    } else {
+      for (uint32_t i = tid; i < valid; i += THREADS) {
+        s.keys[buf][i] = kin[base + i];
+        if (HV) s.vals[buf][i] = vin[base + i];
+      }
+      __syncthreads();
+    }
+
+    // Keys (and values) of this thread, warp-striped from the staged tile.
+    K key[KPT];
+    uint32_t val[KPT];
+    const int sb = warp * 32 * KPT + lane;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const int i = sb + j * 32;
+      key[j] = (i < (int)valid) ? s.keys[buf][i] : ~K(0);
+      if (HV) val[j] = s.vals[buf][i];
+    }
+    // A. early per-warp digit counts.
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      const uint32_t peers = peer_mask<MATCH>(d);
+      if (lane == 31 - __clz(peers)) atomicAdd(&s.cnt[warp][d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    // B. per-digit offsets across warps, tile aggregate, tile-local digit bases.
+    uint32_t count = 0;
+    if (tid < RADIX) {
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = s.cnt[w][tid];
+        s.cnt[w][tid] = count;
+        count += c;
+      }
+      st_relaxed(desc + (size_t)tile * RADIX + tid, (count << 2) | (tile == 0 ? FLAG_INCLUSIVE : FLAG_AGGREGATE));
+    }
+    const uint32_t doff = scan256_exclusive<THREADS>(count, s.warp_sums);
+    if (tid < RADIX) {
+      s.digit_off[tid] = doff;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) s.cnt[w][tid] += doff;
+    }
+    __syncthreads();
+    // C. ranks and scatter into the staged buffer (all reads of it are done).
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      const uint32_t peers = peer_mask<MATCH>(d);
+      const int leader = 31 - __clz(peers);
+      uint32_t b0 = 0;
+      if (lane == leader) b0 = atomicAdd(&s.cnt[warp][d], (uint32_t)__popc(peers));
+      b0 = __shfl_sync(0xffffffffu, b0, leader);
+      const uint32_t pos = b0 + __popc(peers & lt_mask);
+      s.keys[buf][pos] = key[j];
+      if (HV) s.vals[buf][pos] = val[j];
+    }
+    // D. decoupled look-back, one thread per digit.
+    if (tid < RADIX) {
+      uint32_t excl = 0;
+      if (tile > 0) {
+        int k = (int)tile - 1;
+        while (true) {
+          const uint32_t v = spin_descriptor(desc + (size_t)k * RADIX + tid, status);
+          excl += v >> 2;
+          if ((v & 3u) == FLAG_INCLUSIVE || k == 0) break;
+          --k;
+        }
+        st_relaxed(desc + (size_t)tile * RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
+      }
+      s.gbase[tid] = bin_off[tid] + excl - s.digit_off[tid];
+    }
+    __syncthreads();
+    // E. coalesced writes of each digit run.
+    for (uint32_t i = tid; i < valid; i += THREADS) {
+      const K k = s.keys[buf][i];
+      const uint32_t o = s.gbase[(uint32_t)(k >> shift) & dmask] + i;
+      kout[o] = k;
+      if (HV) vout[o] = s.vals[buf][i];
+    }
+    for (int i = tid; i < WARPS * RADIX; i += THREADS) (&s.cnt[0][0])[i] = 0;
+    fence_proxy_async_smem();  // this buffer is refilled by TMA two tiles from now
+    __syncthreads();
+    tile = s.next_tile;
+    buf ^= 1;
+  }
+}
+
 // ------------------------------------------------------------- variants ---
-// Tile shapes compiled in.  The first entry per key width is the default;
-// others are available to the autotuner (gtc_sort_set_variant).
+// Tile shapes compiled in.  kind 0: one tile per CTA (onesweep_kernel);
+// kind 1: persistent TMA, __match_any_sync ranks; kind 2: persistent TMA,
+// ballot ranks.  The autotuner times them per key width
+// (gtc_sort_set_variant); TMA kinds need 16-byte aligned inputs and fall back
+// to kind 0 shapes otherwise.
 struct Variant {
   int threads;
   int kpt;
+  int kind;
 };
-constexpr Variant kVariants[] = {{256, 16}, {384, 16}, {512, 12}};
+constexpr Variant kVariants[] = {{256, 16, 0}, {384, 16, 0}, {512, 12, 0},
+                                 {256, 16, 1}, {256, 16, 2}, {512, 8, 1}, {256, 24, 1}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static int g_variant[2] = {0, 0};  // [u32, u64]
+static int g_variant[2] = {3, 3};  // [u32, u64]
 
 template <class K, int THREADS, int KPT, bool HV>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
@@ -299,19 +505,53 @@ static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin
   return cudaGetLastError();
 }
 
+template <class K, int THREADS, int KPT, bool HV, bool MATCH>
+static cudaError_t launch_tma(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
+                              uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
+                              uint32_t* tile_counter) {
+  using S = TmaSmem<K, THREADS, KPT, HV>;
+  auto kern = onesweep_tma_kernel<K, THREADS, KPT, HV, MATCH>;
+  static int per_sm = 0;  // resident CTAs per SM, per instantiation
+  if (per_sm == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, sizeof(S));
+    if (e != cudaSuccess) return e;
+    per_sm = occ > 0 ? occ : 1;
+  }
+  const uint32_t tiles = ceil_div(n, S::TILE);
+  const uint32_t grid = min(tiles, (uint32_t)(per_sm * L.num_sms));
+  kern<<<grid, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
+                                               L.status);
+  return cudaGetLastError();
+}
+
 template <class K>
 static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin, const uint32_t* vin, K* kout,
                                   uint32_t* vout, uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off,
                                   uint32_t* desc, uint32_t* tc) {
+  // TMA bulk copies need 16-byte aligned sources; other inputs use the
+  // one-tile-per-CTA kernel of the same tile width.
+  const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
+  if (kVariants[v].kind != 0 && !aligned) v = 0;
 #define GTC_OS(T, P)                                                                                     \
   return hv ? launch_one<K, T, P, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)   \
             : launch_one<K, T, P, false>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_TMA(T, P, M)                                                                                     \
+  return hv ? launch_tma<K, T, P, true, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)    \
+            : launch_tma<K, T, P, false, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
   switch (v) {
     case 0: GTC_OS(256, 16);
     case 1: GTC_OS(384, 16);
-    default: GTC_OS(512, 12);
+    case 2: GTC_OS(512, 12);
+    case 3: GTC_TMA(256, 16, true);
+    case 4: GTC_TMA(256, 16, false);
+    case 5: GTC_TMA(512, 8, true);
+    default: GTC_TMA(256, 24, true);
   }
 #undef GTC_OS
+#undef GTC_TMA
 }
 
 template <class K>

@@ -87,6 +87,39 @@ def test_sort_pairs_stable(ctx, key_bits, n):
 
 
 @pytest.mark.parametrize("key_bits", [32, 64])
+def test_sort_every_variant(ctx, key_bits):
+    """Every compiled tile shape / ranking scheme sorts stably, on full and
+    ragged tiles, with and without values, on aligned and unaligned inputs."""
+    import torch
+
+    default = ctx.get_sort_variant(key_bits)
+    try:
+        for v in range(len(ctx.sort_variants())):
+            ctx.set_sort_variant(key_bits, v)
+            for n, words in ((1 << 20, 0), (777_777, 3), (6144 * 3, 1)):
+                keys = W.config3_keys(n, key_bits, and_words=words, seed=v * 10 + n % 7)
+                vals = np.arange(n, dtype=np.uint32)
+                order = np.argsort(keys, kind="stable")
+                k, vv = ctx.sort_pairs(dev(keys), dev(vals))
+                assert np.array_equal(host(k, keys.dtype), keys[order]), (v, n)
+                assert np.array_equal(host(vv, np.uint32), order.astype(np.uint32)), (v, n)
+                k, _ = ctx.sort_pairs(dev(keys), None)
+                assert np.array_equal(host(k, keys.dtype), keys[order]), (v, n, "keys only")
+            # unaligned (offset by one element) views take the non-TMA kernel
+            n = 300_001
+            keys = W.config3_keys(n + 1, key_bits, seed=5)
+            tk = dev(keys)[1:]
+            tv = torch.arange(n + 1, dtype=torch.int32, device="cuda")[1:]
+            k, vv = ctx.sort_pairs(tk, tv)
+            order = np.argsort(keys[1:], kind="stable")
+            assert np.array_equal(host(k.contiguous(), keys.dtype), keys[1:][order]), (v, "unaligned")
+            assert np.array_equal(host(vv.contiguous(), np.uint32), (order + 1).astype(np.uint32)), (v, "unaligned")
+            ctx.device_status()
+    finally:
+        ctx.set_sort_variant(key_bits, default)
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
 def test_sort_bit_ranges_and_keys_only(ctx, key_bits):
     n = 300_001
     keys = W.config3_keys(n, key_bits, seed=77)
