@@ -76,6 +76,32 @@ __device__ __forceinline__ uint32_t spin_descriptor(const uint32_t* p, uint32_t*
   return v;
 }
 
+// Exclusive prefix of one digit over tiles [0, tile) by decoupled look-back
+// over descriptors laid out [tile][RADIX].  Loads a window of W predecessors
+// at once (independent loads, one memory latency per window instead of one
+// per tile) and consumes them nearest-first until an INCLUSIVE descriptor.
+template <int W, int RADIX_>
+__device__ __forceinline__ uint32_t lookback_window(const uint32_t* desc, uint32_t tile, uint32_t digit,
+                                                    uint32_t* status) {
+  uint32_t excl = 0;
+  int k = (int)tile - 1;
+  while (k >= 0) {
+    uint32_t v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+      v[w] = (k - w >= 0) ? ld_relaxed(desc + (size_t)(k - w) * RADIX_ + digit) : FLAG_INCLUSIVE;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      uint32_t x = v[w];
+      if ((x & 3u) == FLAG_NOT_READY) x = spin_descriptor(desc + (size_t)(k - w) * RADIX_ + digit, status);
+      excl += x >> 2;
+      if ((x & 3u) == FLAG_INCLUSIVE) return excl;
+    }
+    k -= W;
+  }
+  return excl;
+}
+
 // ------------------------------------------------ TMA bulk copy / mbarrier --
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

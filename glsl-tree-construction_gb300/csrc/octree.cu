@@ -115,7 +115,6 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
                                                                   gtc_octnode* __restrict__ nodes, uint32_t capacity,
                                                                   uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
-  __shared__ int4 s_stage[OCT_CAP * 4];
   const uint32_t u = d_u ? *d_u : u_host;
   if (u == 0) return;
   const uint32_t m = u - 1;
@@ -134,22 +133,19 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
     return;
   }
   const int root_level = (prefix_n[0] - A) / 3;
-  for (uint32_t kb = blockIdx.x * OCT_THREADS; kb < m; kb += gridDim.x * OCT_THREADS) {
-    // Radix nodes [kb, kend) own the contiguous slots [first, last1).
-    const uint32_t kend = min(kb + (uint32_t)OCT_THREADS, m);
-    const uint32_t first = (kb == 0) ? 0u : ps[kb - 1] + 1;
-    const uint32_t last1 = ps[kend - 1] + 1;
-    const bool staged = last1 >= first && last1 - first <= (uint32_t)OCT_CAP && last1 <= capacity;
-    const NodeSink sink{s_stage, nodes, first, staged};
-    __syncthreads();  // the previous pass's flush has read the staging area
-    const uint32_t k = kb + threadIdx.x;
-    if (k < m) {
+  // The kernel is bound by the latency of its dependent loads (node -> child
+  // -> grandchild), not by bandwidth: one thread per radix node, no block
+  // barriers, 16-byte stores straight to HBM.
+  const NodeSink sink{nullptr, nodes, 0, false};
+  const uint32_t stride = gridDim.x * OCT_THREADS;
+  for (uint32_t k = blockIdx.x * OCT_THREADS + threadIdx.x; k < m; k += stride) {
+    {
       const uint32_t c = edge[k];
       const uint32_t top = ps[k];
       if (k == 0 || c > 0) {
         if (k != 0 && c > top) {  // slot 0 is the root's: inconsistent offsets
           atomicOr(status, DEV_INTERNAL);
-        } else if (!staged && (k == 0 ? 1u : top + 1) > capacity) {
+        } else if ((k == 0 ? 1u : top + 1) > capacity) {
           atomicOr(status, DEV_CAPACITY);
         } else {
           const uint32_t bottom = (k == 0) ? 0u : top - c + 1;
@@ -179,12 +175,6 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
         }
       }
     }
-    __syncthreads();
-    if (staged) {  // coalesced 16-byte stores of the block's contiguous node range
-      int4* dst = reinterpret_cast<int4*>(nodes + first);
-      const uint32_t words = (last1 - first) * 4;
-      for (uint32_t x = threadIdx.x; x < words; x += OCT_THREADS) dst[x] = s_stage[x];
-    }
   }
 }
 
@@ -195,7 +185,7 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
                                gtc_octnode* nodes, uint32_t capacity, bool with_leaves) {
   const uint32_t work = d_u ? n_max : u_host;
   if (work == 0) return cudaSuccess;
-  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 6));
+  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 16));
   if (with_leaves)
     octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left, edge, ps,
                                                              mn, rg, nodes, capacity, L.status);

@@ -199,29 +199,24 @@ __global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__
     if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
   }
 
-  // 3. warp multisplit ranks (stable: j-major then lane order = input order).
-  uint32_t rank[KPT];
+  // 3. early per-warp digit counts: one shared atomic per key (one per warp
+  // when all 32 lanes share the digit, the low-entropy case).
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* my_hist = s.warp_hist[warp];
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-    uint32_t peers = 0xffffffffu;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const uint32_t bit = (d >> b) & 1u;
-      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-      peers &= bit ? bal : ~bal;
+    const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+    if (__all_sync(0xffffffffu, d == d0)) {
+      if (lane == 0) atomicAdd(&my_hist[d], 32u);
+    } else {
+      atomicAdd(&my_hist[d], 1u);
     }
-    const uint32_t base = my_hist[d];
-    __syncwarp();
-    if (lane == 31 - __clz(peers)) my_hist[d] = base + __popc(peers);
-    __syncwarp();
-    rank[j] = base + __popc(peers & lt_mask);
   }
   __syncthreads();
 
-  // 4. per-digit counts across warps; publish the tile aggregate early.
+  // 4. per-digit counts across warps; publish the tile aggregate early; turn
+  // the per-warp counts into tile-local start positions.
   uint32_t count = 0;
   if (tid < RADIX) {
 #pragma unroll
@@ -233,34 +228,47 @@ __global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__
     st_relaxed(desc + (size_t)tile * RADIX + tid, (count << 2) | (tile == 0 ? FLAG_INCLUSIVE : FLAG_AGGREGATE));
   }
   const uint32_t digit_off = scan256_exclusive<THREADS>(count, s.warp_sums);
-
-  // 5. decoupled look-back over predecessor tiles, one thread per digit.
   if (tid < RADIX) {
     s.digit_offset[tid] = digit_off;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) s.warp_hist[w][tid] += digit_off;
+  }
+  __syncthreads();
+
+  // 5. stable ranks by warp multisplit (8 __ballot_sync give the peer mask;
+  // the highest peer advances the warp's digit cursor and broadcasts the old
+  // value) and the scatter into tile-local digit order.
+#pragma unroll
+  for (int j = 0; j < KPT; ++j) {
+    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint32_t bit = (d >> b) & 1u;
+      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? bal : ~bal;
+    }
+    const int leader = 31 - __clz(peers);
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    const uint32_t local = base + __popc(peers & lt_mask);
+    s.keys[local] = key[j];
+    if (HAS_VALS) s.vals[local] = val[j];
+  }
+
+  // 6. decoupled look-back over predecessor tiles, one thread per digit.
+  if (tid < RADIX) {
     uint32_t excl = 0;
     if (tile > 0) {
-      int k = (int)tile - 1;
-      while (true) {
-        const uint32_t v = spin_descriptor(desc + (size_t)k * RADIX + tid, status);
-        excl += v >> 2;
-        if ((v & 3u) == FLAG_INCLUSIVE || k == 0) break;
-        --k;
-      }
+      excl = lookback_window<8, RADIX>(desc, tile, tid, status);
       st_relaxed(desc + (size_t)tile * RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
     }
     s.global_base[tid] = bin_off[tid] + excl - digit_off;
   }
   __syncthreads();
 
-  // 6. scatter into tile-local digit order, then coalesced run writes.
-#pragma unroll
-  for (int j = 0; j < KPT; ++j) {
-    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-    const uint32_t local = s.digit_offset[d] + my_hist[d] + rank[j];
-    s.keys[local] = key[j];
-    if (HAS_VALS) s.vals[local] = val[j];
-  }
-  __syncthreads();
+  // 7. coalesced writes of each digit run.
   const uint32_t valid = min((uint32_t)TILE, n - tile_base);
   for (uint32_t i = tid; i < valid; i += THREADS) {
     const K k = s.keys[i];
@@ -401,12 +409,17 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tm
       key[j] = (i < (int)valid) ? s.keys[buf][i] : ~K(0);
       if (HV) val[j] = s.vals[buf][i];
     }
-    // A. early per-warp digit counts.
+    // A. early per-warp digit counts (shared atomics; one per warp when all
+    // lanes share the digit).
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
       const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-      const uint32_t peers = peer_mask<MATCH>(d);
-      if (lane == 31 - __clz(peers)) atomicAdd(&s.cnt[warp][d], (uint32_t)__popc(peers));
+      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+      if (__all_sync(0xffffffffu, d == d0)) {
+        if (lane == 0) atomicAdd(&s.cnt[warp][d], 32u);
+      } else {
+        atomicAdd(&s.cnt[warp][d], 1u);
+      }
     }
     __syncthreads();
     // B. per-digit offsets across warps, tile aggregate, tile-local digit bases.
@@ -444,13 +457,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tm
     if (tid < RADIX) {
       uint32_t excl = 0;
       if (tile > 0) {
-        int k = (int)tile - 1;
-        while (true) {
-          const uint32_t v = spin_descriptor(desc + (size_t)k * RADIX + tid, status);
-          excl += v >> 2;
-          if ((v & 3u) == FLAG_INCLUSIVE || k == 0) break;
-          --k;
-        }
+        excl = lookback_window<8, RADIX>(desc, tile, tid, status);
         st_relaxed(desc + (size_t)tile * RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
       }
       s.gbase[tid] = bin_off[tid] + excl - s.digit_off[tid];
@@ -483,9 +490,9 @@ struct Variant {
   int kind;
 };
 constexpr Variant kVariants[] = {{256, 16, 0}, {384, 16, 0}, {512, 12, 0},
-                                 {256, 16, 1}, {256, 16, 2}, {512, 8, 1}, {256, 24, 1}};
+                                 {256, 16, 1}, {256, 16, 2}, {512, 8, 2}, {256, 24, 2}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static int g_variant[2] = {3, 3};  // [u32, u64]
+static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 before autotuning
 
 template <class K, int THREADS, int KPT, bool HV>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
@@ -547,8 +554,8 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
     case 2: GTC_OS(512, 12);
     case 3: GTC_TMA(256, 16, true);
     case 4: GTC_TMA(256, 16, false);
-    case 5: GTC_TMA(512, 8, true);
-    default: GTC_TMA(256, 24, true);
+    case 5: GTC_TMA(512, 8, false);
+    default: GTC_TMA(256, 24, false);
   }
 #undef GTC_OS
 #undef GTC_TMA

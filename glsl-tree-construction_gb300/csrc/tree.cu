@@ -9,9 +9,10 @@
 //     drops the last key);
 //   * exponential + binary search for the range end j, binary search for the
 //     split gamma, leaf flags, parent scatter.
-// The searches are dependent loads; most ranges are short, so each block
-// stages the codes of its tile plus a halo on either side in shared memory
-// and only the rare long searches go to global memory (L2).
+// The kernel is bound by instruction issue (the searches are data-dependent
+// loops), so all index arithmetic is 32-bit (u < 2^30) and the code loads go
+// through the read-only L1 path, which serves the short searches that make
+// up most nodes.
 // The edge count of edge_count.comp:30-41 needs depth(parent): a node knows
 // the exact key ranges of both children ([lo, gamma] and [gamma + 1, hi]),
 // so it computes each internal child's prefix length from the range ends and
@@ -22,9 +23,6 @@
 namespace gtc {
 
 constexpr int TREE_THREADS = 256;
-constexpr int TREE_NPT = 8;                            // nodes per thread per tile
-constexpr int TREE_TILE = TREE_THREADS * TREE_NPT;     // 2048 nodes
-constexpr int TREE_HALO = 1024;                        // staged codes on each side
 
 template <class K>
 __global__ void __launch_bounds__(TREE_THREADS) radix_tree_kernel(const K* __restrict__ codes, const uint32_t* d_u,
@@ -35,8 +33,7 @@ __global__ void __launch_bounds__(TREE_THREADS) radix_tree_kernel(const K* __res
                                                                   int32_t* __restrict__ parent,
                                                                   uint32_t* __restrict__ edge, uint32_t* d_m) {
   constexpr int A = KeyTraits<K>::A;
-  __shared__ K s_codes[TREE_TILE + 2 * TREE_HALO + 1];
-  const int64_t m = d_u ? (int64_t)max(*d_u, 1u) - 1 : (int64_t)m_host;
+  const int m = d_u ? (int)max(*d_u, 1u) - 1 : m_host;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (d_m) *d_m = (uint32_t)m;
     if (m > 0) {
@@ -44,72 +41,60 @@ __global__ void __launch_bounds__(TREE_THREADS) radix_tree_kernel(const K* __res
       if (edge) edge[0] = 0;
     }
   }
-  for (int64_t tb = (int64_t)blockIdx.x * TREE_TILE; tb < m; tb += (int64_t)gridDim.x * TREE_TILE) {
-    // Window [wlo, whi] of codes (code indices run 0..m).
-    const int64_t wlo = tb > TREE_HALO ? tb - TREE_HALO : 0;
-    const int64_t whi = min(tb + TREE_TILE + TREE_HALO, m);
-    __syncthreads();
-    for (int64_t x = wlo + threadIdx.x; x <= whi; x += TREE_THREADS) s_codes[x - wlo] = codes[x];
-    __syncthreads();
-    auto C = [&](int64_t x) -> K { return (x >= wlo && x <= whi) ? s_codes[x - wlo] : __ldg(codes + x); };
-#pragma unroll 1
-    for (int r = 0; r < TREE_NPT; ++r) {
-      const int64_t i = tb + (int64_t)r * TREE_THREADS + threadIdx.x;
-      if (i >= m) break;
-      const K ci = C(i);
-      int d = 1;
-      if (i > 0) {
-        const int dr = delta_key(ci, C(i + 1));
-        const int dl = delta_key(ci, C(i - 1));
-        d = (dr > dl) - (dr < dl);
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+    const K ci = __ldg(codes + i);
+    int d = 1;
+    if (i > 0) {
+      const int dr = delta_key(ci, __ldg(codes + i + 1));
+      const int dl = delta_key(ci, __ldg(codes + i - 1));
+      d = (dr > dl) - (dr < dl);
+    }
+    // Range length l (in keys) away from i in direction d.
+    uint32_t l = 0;
+    if (i == 0) {
+      l = (uint32_t)m;
+    } else {
+      const int dmin = delta_key(ci, __ldg(codes + i - d));
+      const uint32_t lim = (d > 0) ? (uint32_t)(m - i) : (uint32_t)i;  // farthest reachable step
+      uint32_t lmax = 2;
+      while (lmax <= lim && delta_key(ci, __ldg(codes + i + (int)lmax * d)) > dmin) lmax <<= 1;
+      for (uint32_t t = lmax >> 1; t >= 1; t >>= 1) {
+        if (l + t <= lim && delta_key(ci, __ldg(codes + i + (int)(l + t) * d)) > dmin) l += t;
       }
-      int64_t l = 0;
-      if (i == 0) {
-        l = m;
-      } else {
-        const int dmin = delta_key(ci, C(i - d));
-        int64_t lmax = 2;
-        while (true) {
-          const int64_t p = i + lmax * d;
-          if (p < 0 || p > m) break;
-          if (delta_key(ci, C(p)) <= dmin) break;
-          lmax *= 2;
-        }
-        const int64_t lcut = (d == -1) ? i : m - i;
-        for (int64_t t = lmax >> 1; t >= 1; t >>= 1) {
-          if (l + t <= lcut && delta_key(ci, C(i + (l + t) * d)) > dmin) l += t;
-        }
+    }
+    const int j = i + (int)l * d;
+    const int dnode = delta_key(ci, __ldg(codes + j));
+    // Split search: t = ceil(l / 2^k) for 2^k up to 2^ceil(log2 l).
+    uint32_t s = 0;
+    if (l > 1) {
+      // The shader bounds s + t by the array (i - 1 or m - i - 1); a probe at
+      // s + t == l lands on the range end, whose delta equals dnode and never
+      // advances s, so bounding by l - 1 gives the same split.
+      const uint32_t scut = l - 1;
+      const int lg = 32 - __clz(l - 1);  // ceil(log2 l)
+      for (int k = 1; k <= lg; ++k) {
+        const uint32_t t = (l + (1u << k) - 1) >> k;
+        if (s + t <= scut && delta_key(ci, __ldg(codes + i + (int)(s + t) * d)) > dnode) s += t;
       }
-      const int64_t j = i + l * d;
-      const int dnode = delta_key(ci, C(j));
-      // Split search: t = ceil(l / 2^k) for 2^k up to 2^ceil(log2 l).
-      int64_t s = 0;
-      const int64_t scut = (d == -1) ? i - 1 : m - i - 1;
-      if (l > 1) {
-        const int lg = 64 - __clzll((unsigned long long)(l - 1));  // ceil(log2 l)
-        for (int k = 1; k <= lg; ++k) {
-          const int64_t t = (l + ((int64_t)1 << k) - 1) >> k;
-          if (s + t <= scut && delta_key(ci, C(i + (s + t) * d)) > dnode) s += t;
-        }
-      }
-      const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
-      const int64_t lo = d > 0 ? i : j;
-      const int64_t hi = d > 0 ? j : i;
-      const bool leaf_l = (lo == gamma);
-      const bool leaf_r = (hi == gamma + 1);
-      prefix_n[i] = (uint8_t)dnode;
-      left[i] = (int32_t)gamma;
-      hll[i] = leaf_l;
-      hlr[i] = leaf_r;
-      const int depth_i = (dnode - A) / 3;
-      if (!leaf_l) {
-        parent[gamma] = (int32_t)i;
-        if (edge) edge[gamma] = (uint32_t)((delta_key(C(lo), C(gamma)) - A) / 3 - depth_i);
-      }
-      if (!leaf_r) {
-        parent[gamma + 1] = (int32_t)i;
-        if (edge) edge[gamma + 1] = (uint32_t)((delta_key(C(gamma + 1), C(hi)) - A) / 3 - depth_i);
-      }
+    }
+    const int gamma = i + (int)s * d + (d < 0 ? -1 : 0);
+    const int lo = d > 0 ? i : j;
+    const int hi = d > 0 ? j : i;
+    const bool leaf_l = (lo == gamma);
+    const bool leaf_r = (hi == gamma + 1);
+    prefix_n[i] = (uint8_t)dnode;
+    left[i] = gamma;
+    hll[i] = leaf_l;
+    hlr[i] = leaf_r;
+    const int depth_i = (dnode - A) / 3;
+    if (!leaf_l) {
+      parent[gamma] = i;
+      if (edge) edge[gamma] = (uint32_t)((delta_key(__ldg(codes + lo), __ldg(codes + gamma)) - A) / 3 - depth_i);
+    }
+    if (!leaf_r) {
+      parent[gamma + 1] = i;
+      if (edge) edge[gamma + 1] = (uint32_t)((delta_key(__ldg(codes + gamma + 1), __ldg(codes + hi)) - A) / 3 - depth_i);
     }
   }
 }
@@ -120,7 +105,7 @@ cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d
                               uint32_t* edge, uint32_t* d_m) {
   const uint32_t work = d_u ? n_max : (uint32_t)max(m_host, 0);
   if (work == 0 && !d_m) return cudaSuccess;
-  const uint32_t grid = max(1u, min(ceil_div(work, TREE_TILE), (uint32_t)L.num_sms * 6));
+  const uint32_t grid = max(1u, min(ceil_div(work, TREE_THREADS), (uint32_t)L.num_sms * 8));
   radix_tree_kernel<K><<<grid, TREE_THREADS, 0, L.stream>>>(codes, d_u, m_host, prefix_n, hll, hlr, left, parent,
                                                              edge, d_m);
   return cudaGetLastError();
