@@ -46,7 +46,7 @@ def parse_args():
     ap.add_argument("--impl", choices=["gtc", "reference"], default="gtc")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (default: the 10M workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["octree", "sort"], default="octree",
+    ap.add_argument("--workload", choices=["octree", "sort", "learned"], default="octree",
                     help="octree: the 10M clustered full build (default); sort: onesweep pairs sort only")
     ap.add_argument("--key-bits", type=int, default=64, help="sort workload: 32 or 64")
     ap.add_argument("--and-words", type=int, default=0, help="sort workload: AND of k uniform words (0 = uniform)")
@@ -421,12 +421,123 @@ def run_gtc_sort(args):
     ctx.close()
 
 
+def run_gtc_learned(args):
+    """Learned-bucket sort vs plain onesweep on clustered 64-bit Morton keys
+    (64-component Gaussian mixture, sigma 0.3-3% of the domain, Dirichlet(1)
+    weights, 5% noise).  The model is trained on a 1% sample of a prior run's
+    sorted keys (same mixture, another seed); both sorts must give identical
+    output; a shifted mixture must take the onesweep fallback."""
+    import numpy as np
+    import torch
+
+    import gtc
+    from gtc import workloads as W
+
+    n = args.n
+    ctx = gtc.Context(0)
+    stream = torch.cuda.current_stream()
+
+    def keys_of(seed, shifted=False, count=n):
+        pts = torch.from_numpy(W.config5_points(count, seed=seed, shifted=shifted)).cuda()
+        k, _ = ctx.morton(pts, 64, with_idx=False)
+        del pts
+        return k
+
+    prior = keys_of(1)
+    ctx.sort_pairs(prior, None, 0, 64)  # the pipeline's own previous sort
+    B = gtc.learned_buckets_for(n)
+    model = gtc.LearnedModel(ctx, B)
+    t0 = time.perf_counter()
+    loss = model.train(prior, stride=100, iters=100, lr=1e-4)
+    train_s = time.perf_counter() - t0
+    del prior
+    keys = keys_of(2)
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    ko, vo = torch.empty_like(keys), torch.empty_like(vals)
+    ws = ctx.workspace(gtc.OP_LEARNED_SORT, n, 64)
+    flags = None
+    wk, wv = torch.empty_like(keys), torch.empty_like(vals)
+    ka, va = torch.empty_like(keys), torch.empty_like(vals)
+    sws = ctx.workspace(gtc.OP_SORT_PAIRS, n, 64)
+
+    def learned_step():
+        nonlocal flags
+        _, _, flags = model.sort(keys, vals, ws=ws, keys_out=ko, vals_out=vo)
+
+    def plain_step():
+        ctx.sort_pairs(wk, wv, 0, 64, ws=sws, keys_alt=ka, vals_alt=va)
+
+    def timed(step, restore=None):
+        for _ in range(max(args.warmup, 3)):
+            if restore:
+                restore()
+            step()
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(args.steps):
+            if restore:
+                restore()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / args.steps
+
+    def restore():
+        wk.copy_(keys)
+        wv.copy_(vals)
+
+    with ClockSampler(0) as clk:
+        learned_ms = timed(learned_step)
+        plain_ms = timed(plain_step, restore)
+    fl = int(flags.item())
+    identical = bool(torch.equal(ko, wk) and torch.equal(vo, wv))
+    ctx.device_status()
+    # A distribution the model was not trained on must fall back, exactly.
+    shifted = keys_of(3, shifted=True, count=min(n, 8_000_000))
+    sko, svo, sflags = model.sort(shifted)
+    sk2, sv2 = shifted.clone(), torch.arange(shifted.numel(), dtype=torch.int32, device="cuda")
+    ctx.sort_pairs(sk2, sv2, 0, 64)
+    shifted_ok = bool(torch.equal(sko, sk2) and torch.equal(svo, sv2))
+    counts = model.histogram(keys).cpu().numpy()
+    top = torch.bincount((keys >> 52).to(torch.int64), minlength=4096).cpu().numpy()
+    peak, peak_kind = measured_hbm_peak()
+    # compulsory bytes of the learned path per key: count read 8, scatter
+    # read 12 + write 16, bucket sort read 16 + write 12
+    lbytes = 64 * n
+    line = {
+        "metric": "Mkeys/s learned-bucket sort", "value": round(n / (learned_ms * 1e-3) / 1e6, 2), "unit": "Mkeys/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(learned_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"learned_sort_u64_n{n}", "buckets": B, "train_loss": loss,
+                   "train_s": round(train_s, 3), "flags": fl, "identical_to_onesweep": identical,
+                   "plain_onesweep_mkeys_s": round(n / (plain_ms * 1e-3) / 1e6, 2),
+                   "plain_ms": round(plain_ms, 4), "speedup_vs_plain": round(plain_ms / learned_ms, 3),
+                   "shifted_flags": int(sflags.item()), "shifted_exact": shifted_ok,
+                   "bucket_max_over_mean": round(float(counts.max() / (n / B)), 3),
+                   "topbits_max_over_mean": round(float(top.max() / (n / 4096)), 3)},
+        "roofline": {"bound": "hbm", "kernel": "learned path (count + scatter + bucket sort)",
+                     "achieved": round(lbytes / (learned_ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(lbytes / (learned_ms * 1e-3) / 1e9 / peak, 4), "traffic": None,
+                     "peak_kind": peak_kind},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    model.close()
+    ctx.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "sort":
         run_gtc_sort(args)
+    elif args.workload == "learned":
+        run_gtc_learned(args)
     else:
         run_gtc(args)
 

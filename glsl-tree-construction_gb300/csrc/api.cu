@@ -490,6 +490,10 @@ GTC_API gtc_status gtc_workspace_size(gtc_ctx* ctx, gtc_op op, uint32_t n, int k
     case GTC_OP_BUILD_OCTREE:
       *bytes = key_bits == 64 ? pipeline_ws_bytes<uint64_t>(n) : pipeline_ws_bytes<uint32_t>(n);
       return GTC_OK;
+    case GTC_OP_LEARNED_SORT:
+      if (key_bits != 64) return fail(ctx, GTC_ERR_INVALID_ARG, "the learned sort takes 64-bit keys");
+      *bytes = learned_workspace_bytes(n);
+      return GTC_OK;
   }
   return fail(ctx, GTC_ERR_INVALID_ARG, "unknown op");
 }

@@ -234,6 +234,10 @@ struct Launch {
   cudaStream_t stream;
   uint32_t* status;  // device status word
   int num_sms;
+  // Sort kernels launched with run_if set do their work only when *run_if is
+  // nonzero (a decision taken on the device, e.g. the learned sort's
+  // fallback), so a stream or graph can hold them unconditionally.
+  const uint32_t* run_if = nullptr;
 };
 
 // Sort tuning knobs, chosen from the compiled variant table.
@@ -279,6 +283,7 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
 
 // Decoupled look-back scans: unique compaction and node offsets.
 size_t scan_workspace_bytes(uint32_t n);
+size_t learned_workspace_bytes(uint32_t n);
 template <class K>
 cudaError_t launch_unique(const Launch& L, const K* keys_in, const uint32_t* vals_in, K* keys_out,
                           uint32_t* vals_out, uint32_t n, uint32_t* d_count, void* ws);

@@ -1,0 +1,786 @@
+// learned.cu - learned-bucket sort of 64-bit keys with a u32 payload.
+//
+// No counterpart in the reference (its sort is the onesweep of
+// new_radix_sort.comp); the output is defined to be exactly the stable
+// onesweep result.
+//
+// Model: a piecewise-linear CDF with B segments (one per bucket).  The B + 1
+// knots are u64 keys at quantiles of a 1% sample of a previously sorted key
+// set; the B + 1 FP32 heights are trained on the GPU by the forward / backward
+// / Adam kernels below (mean squared error against the sample's empirical
+// CDF).  bucket(key) = floor(B * F(key)), with F clamped inside each segment
+// so that F, and therefore the bucket, is monotone in the key whenever the
+// heights are non-decreasing (the update projects them so).
+//
+// Sort (all stream-ordered, decisions on the device):
+//   1. count:   per 64K-key tile, B-bin shared histogram of model buckets;
+//   2. scan:    per-bucket offsets over tiles, bucket bases; a bucket larger
+//               than the on-chip capacity sets the OVERFLOW flag;
+//   3. scatter: each key (with its value and position) to its bucket segment;
+//   4. bucket sort: one CTA per bucket sorts its segment in shared memory
+//               (LSD over the bits that vary inside the bucket, then equal
+//               keys ordered by original position) and writes the output;
+//   5. check:   consecutive non-empty buckets must hold increasing key ranges
+//               (ORDER flag);
+//   6. fallback: with any flag set, the input is copied to the output and the
+//               plain onesweep kernels (launched unconditionally, gated on the
+//               flag word) sort it; otherwise they return at once.
+
+#include <cstdio>
+#include <new>
+
+#include "gtc_internal.cuh"
+
+namespace gtc {
+
+Launch context_launch(gtc_ctx* ctx, gtc_stream_t stream);
+gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_t e);
+
+constexpr uint32_t LFLAG_OVERFLOW = 1u;   // a bucket exceeds the on-chip sort capacity
+constexpr uint32_t LFLAG_ORDER = 2u;      // bucket key ranges out of order
+constexpr uint32_t LFLAG_BAD_MODEL = 4u;  // heights not non-decreasing
+constexpr uint32_t LFLAG_DUP_RUN = 8u;    // a run of equal keys too long to order on chip
+
+constexpr int LC_THREADS = 1024;
+constexpr int LC_KPT = 64;
+constexpr int LC_TILE = LC_THREADS * LC_KPT;  // 65536 keys per count/scatter tile
+constexpr int BS_THREADS = 1024;
+constexpr int BS_CAP = 16384;                 // keys per bucket sorted on chip (229,920 B of smem)
+constexpr int BS_MAX_RUN = 256;
+constexpr int MAX_BUCKETS = 8192;  // knots + heights + histogram must fit one CTA's shared memory
+
+// ---------------------------------------------------------------- model ---
+// The interior knots kn[1..B-1] (B a power of two: a perfect binary tree) are
+// also kept in breadth-first (Eytzinger) order e[1..B-1], so the lanes of a
+// warp that walk down the tree read consecutive words at every level instead
+// of striding through one shared-memory bank as a plain binary search over a
+// power-of-two array does.
+__device__ __forceinline__ void build_eytzinger(uint64_t* e, const uint64_t* kn, int B) {
+  const int d = 31 - __clz(B);
+  for (int i = threadIdx.x; i < B; i += blockDim.x) {
+    if (i == 0) continue;
+    const int L = 31 - __clz(i);
+    const int rank = ((2 * (i - (1 << L)) + 1) << (d - 1 - L)) - 1;  // in-order position
+    e[i] = kn[rank + 1];
+  }
+}
+
+__device__ __forceinline__ int model_bucket(uint64_t key, const uint64_t* e, const uint64_t* kn, const float* y,
+                                            int B) {
+  int i = 1;
+  while (i < B) i = 2 * i + (e[i] <= key ? 1 : 0);
+  const int lo = i - B;  // interior knots <= key == segment index (kn[0] == 0)
+  const uint64_t k0 = kn[lo], k1 = kn[lo + 1];
+  const float y0 = y[lo], y1 = y[lo + 1];
+  const float w = (k1 > k0) ? __fdiv_rn((float)(key - k0), (float)(k1 - k0)) : 0.0f;
+  float F = __fadd_rn(y0, __fmul_rn(__fsub_rn(y1, y0), w));
+  F = fminf(fmaxf(F, y0), y1);
+  const int b = __float2int_rz(__fmul_rn(F, (float)B));
+  return min(max(b, 0), B - 1);
+}
+
+// Segment of a key and its interpolation weight (the training forward pass).
+__device__ __forceinline__ int model_segment(uint64_t key, const uint64_t* kn, int B, float* w) {
+  int lo = 0, hi = B;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (kn[mid] <= key) lo = mid;
+    else hi = mid;
+  }
+  const uint64_t k0 = kn[lo], k1 = kn[lo + 1];
+  *w = (k1 > k0) ? __fdiv_rn((float)(key - k0), (float)(k1 - k0)) : 0.0f;
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* a, uint32_t n, uint64_t x) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------- training ---
+__global__ void sample_kernel(const uint64_t* sorted, uint32_t ns, uint32_t stride, uint64_t* sample) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += gridDim.x * blockDim.x)
+    sample[j] = sorted[(size_t)j * stride];
+}
+
+__global__ void knots_init_kernel(const uint64_t* sample, uint32_t ns, int B, uint64_t* kn, float* y, float* m1,
+                                  float* m2) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= B; b += gridDim.x * blockDim.x) {
+    uint64_t k;
+    if (b == 0) k = 0;
+    else if (b == B) k = ~0ull;
+    else k = sample[(uint64_t)b * ns / (uint32_t)B];
+    kn[b] = k;
+    y[b] = (float)b / (float)B;
+    m1[b] = 0.0f;
+    m2[b] = 0.0f;
+  }
+}
+
+// Forward: mean squared error of F against t_j = (j + 0.5) / ns.
+__global__ void loss_kernel(const uint64_t* sample, uint32_t ns, const uint64_t* kn, const float* y, int B,
+                            float* loss) {
+  __shared__ float s_part[32];
+  float acc = 0.0f;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += gridDim.x * blockDim.x) {
+    float w;
+    const int s = model_segment(sample[j], kn, B, &w);
+    const float F = y[s] + (y[s + 1] - y[s]) * w;
+    const float r = F - ((float)j + 0.5f) / (float)ns;
+    acc += r * r;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = (threadIdx.x < blockDim.x / 32) ? s_part[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) atomicAdd(loss, v / (float)ns);
+  }
+}
+
+// Backward: dL/dy_k = (2 / ns) * [sum over segment k of r (1 - w) + sum over
+// segment k-1 of r w].  One thread per knot; the sample is sorted, so each
+// segment is a contiguous index range found by binary search; sums run in
+// index order (deterministic).
+__global__ void grad_kernel(const uint64_t* sample, uint32_t ns, const uint64_t* kn, const float* y, int B,
+                            float* grad) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= B; k += gridDim.x * blockDim.x) {
+    float g = 0.0f;
+    for (int s = k - 1; s <= k; ++s) {
+      if (s < 0 || s >= B) continue;
+      const uint32_t a = lower_bound_u64(sample, ns, kn[s]);
+      const uint32_t e = (s + 1 == B) ? ns : lower_bound_u64(sample, ns, kn[s + 1]);
+      const uint64_t k0 = kn[s], k1 = kn[s + 1];
+      const float y0 = y[s], y1 = y[s + 1];
+      for (uint32_t j = a; j < e; ++j) {
+        const float w = (k1 > k0) ? __fdiv_rn((float)(sample[j] - k0), (float)(k1 - k0)) : 0.0f;
+        const float r = y0 + (y1 - y0) * w - ((float)j + 0.5f) / (float)ns;
+        g += (s == k) ? r * (1.0f - w) : r * w;
+      }
+    }
+    grad[k] = 2.0f * g / (float)ns;
+  }
+}
+
+// Adam step on the heights, then projection: y_0 = 0, y_B = 1, clamp to
+// [0, 1], running maximum so the heights are non-decreasing.  One block.
+__global__ void __launch_bounds__(1024) adam_kernel(float* y, const float* grad, float* m1, float* m2, int B, float lr,
+                                                    int step) {
+  __shared__ float s_max[1024];
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-12f;
+  const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+  const int n = B + 1;
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int first = threadIdx.x * per;
+  float run = 0.0f;
+  for (int i = first; i < min(first + per, n); ++i) {
+    const float g = grad[i];
+    const float a = b1 * m1[i] + (1.0f - b1) * g;
+    const float v = b2 * m2[i] + (1.0f - b2) * g * g;
+    m1[i] = a;
+    m2[i] = v;
+    float yi = y[i] - lr * (a / c1) / (sqrtf(v / c2) + eps);
+    yi = (i == 0) ? 0.0f : (i == B ? 1.0f : fminf(fmaxf(yi, 0.0f), 1.0f));
+    run = fmaxf(run, yi);
+    y[i] = run;  // running max within the chunk
+  }
+  s_max[threadIdx.x] = run;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {  // inclusive max-scan of chunk maxima
+    const float t = (threadIdx.x >= (unsigned)o) ? s_max[threadIdx.x - o] : 0.0f;
+    __syncthreads();
+    s_max[threadIdx.x] = fmaxf(s_max[threadIdx.x], t);
+    __syncthreads();
+  }
+  const float before = threadIdx.x > 0 ? s_max[threadIdx.x - 1] : 0.0f;
+  for (int i = first; i < min(first + per, n); ++i) y[i] = fmaxf(y[i], before);
+}
+
+// --------------------------------------------------------------- sorting --
+struct ModelSmem {
+  uint64_t* kn;
+  float* y;
+};
+
+__device__ __forceinline__ void load_model(uint64_t* s_kn, float* s_y, const uint64_t* kn, const float* y, int B) {
+  for (int i = threadIdx.x; i <= B; i += blockDim.x) {
+    s_kn[i] = kn[i];
+    s_y[i] = y[i];
+  }
+}
+
+__global__ void __launch_bounds__(LC_THREADS) learned_count_kernel(const uint64_t* __restrict__ keys, uint32_t n,
+                                                                   const uint64_t* kn, const float* y, int B,
+                                                                   uint32_t* counts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* s_kn = s_e + B;
+  float* s_y = reinterpret_cast<float*>(s_kn + (B + 1));
+  uint32_t* s_hist = reinterpret_cast<uint32_t*>(s_y + (B + 1));
+  load_model(s_kn, s_y, kn, y, B);
+  build_eytzinger(s_e, kn, B);
+  for (int b = threadIdx.x; b < B; b += LC_THREADS) s_hist[b] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * LC_TILE;
+#pragma unroll 4
+  for (int j = 0; j < LC_KPT; ++j) {
+    const size_t i = base + (size_t)j * LC_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&s_hist[model_bucket(__ldcs(keys + i), s_e, s_kn, s_y, B)], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += LC_THREADS) counts[(size_t)blockIdx.x * B + b] = s_hist[b];
+}
+
+// Thread per bucket: exclusive offsets over tiles (in place), totals and the
+// capacity check; the last block scans the totals into bucket bases.
+__global__ void __launch_bounds__(1024) learned_scan_kernel(uint32_t* counts, uint32_t tiles, int B, const float* y,
+                                                            uint32_t* totals, uint32_t* base, uint32_t* flags,
+                                                            uint32_t* done) {
+  __shared__ uint32_t s_part[1024];
+  __shared__ uint32_t s_last;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < B) {
+    uint32_t run = 0;
+    for (uint32_t t = 0; t < tiles; ++t) {
+      const uint32_t c = counts[(size_t)t * B + b];
+      counts[(size_t)t * B + b] = run;
+      run += c;
+    }
+    totals[b] = run;
+    if (run > (uint32_t)BS_CAP) atomicOr(flags, LFLAG_OVERFLOW);
+    if (y[b] > y[b + 1]) atomicOr(flags, LFLAG_BAD_MODEL);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1) ? 1u : 0u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int per = (B + 1023) / 1024;
+  const int first = threadIdx.x * per;
+  uint32_t sum = 0;
+  for (int i = first; i < min(first + per, B); ++i) sum += __ldcg(totals + i);
+  s_part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan of the chunk sums
+    const uint32_t t = (threadIdx.x >= (unsigned)o) ? s_part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    s_part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x > 0 ? s_part[threadIdx.x - 1] : 0u;
+  for (int i = first; i < min(first + per, B); ++i) {
+    base[i] = run;
+    run += __ldcg(totals + i);
+  }
+  if (threadIdx.x == 0) *done = 0;
+}
+
+__global__ void __launch_bounds__(LC_THREADS) learned_scatter_kernel(
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, const uint64_t* kn,
+    const float* y, int B, const uint32_t* counts, const uint32_t* base, uint64_t* __restrict__ tkeys,
+    uint32_t* __restrict__ tvals, uint32_t* __restrict__ tpos, const uint32_t* flags) {
+  if (*flags) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* s_kn = s_e + B;
+  float* s_y = reinterpret_cast<float*>(s_kn + (B + 1));
+  uint32_t* s_off = reinterpret_cast<uint32_t*>(s_y + (B + 1));
+  load_model(s_kn, s_y, kn, y, B);
+  build_eytzinger(s_e, kn, B);
+  for (int b = threadIdx.x; b < B; b += LC_THREADS) s_off[b] = base[b] + counts[(size_t)blockIdx.x * B + b];
+  __syncthreads();
+  const size_t tile0 = (size_t)blockIdx.x * LC_TILE;
+#pragma unroll 4
+  for (int j = 0; j < LC_KPT; ++j) {
+    const size_t i = tile0 + (size_t)j * LC_THREADS + threadIdx.x;
+    if (i < n) {
+      const uint64_t k = __ldcs(keys + i);
+      const uint32_t r = atomicAdd(&s_off[model_bucket(k, s_e, s_kn, s_y, B)], 1u);
+      tkeys[r] = k;
+      tvals[r] = vals ? __ldcs(vals + i) : (uint32_t)i;
+      tpos[r] = (uint32_t)i;
+    }
+  }
+}
+
+struct BucketSmem {
+  uint64_t keys[BS_CAP];
+  uint16_t idx[2][BS_CAP];
+  uint32_t hist[BS_THREADS / 32][256];
+  uint32_t warp_sums[8];
+  uint64_t red[64];
+  uint32_t skip;
+};
+
+// One CTA per bucket: LSD counting sort (8-bit digits) of the bucket's key
+// indices in shared memory over the bits that vary inside the bucket, then
+// runs of equal keys ordered by original position, then the output.
+__global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
+    const uint64_t* __restrict__ tkeys, const uint32_t* __restrict__ tvals, const uint32_t* __restrict__ tpos,
+    const uint32_t* base, const uint32_t* totals, uint64_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
+    uint64_t* bmin, uint64_t* bmax, uint32_t* flags) {
+  if (*flags & (LFLAG_OVERFLOW | LFLAG_BAD_MODEL)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  BucketSmem& s = *reinterpret_cast<BucketSmem*>(smem_raw);
+  constexpr int WARPS = BS_THREADS / 32;
+  constexpr int IPT = BS_CAP / BS_THREADS;  // 12 positions per thread
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const int b = blockIdx.x;
+  const uint32_t cnt = totals[b];
+  const uint32_t off = base[b];
+  if (cnt == 0) {
+    if (tid == 0) {
+      bmin[b] = ~0ull;
+      bmax[b] = 0;
+    }
+    return;
+  }
+  if (cnt > (uint32_t)BS_CAP) {
+    if (tid == 0) atomicOr(flags, LFLAG_OVERFLOW);
+    return;
+  }
+  uint64_t mn = ~0ull, mx = 0;
+  for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+    const uint64_t k = tkeys[off + i];
+    s.keys[i] = k;
+    s.idx[0][i] = (uint16_t)i;
+    mn = min(mn, k);
+    mx = max(mx, k);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if (lane == 0) {
+    s.red[warp] = mn;
+    s.red[32 + warp] = mx;
+  }
+  __syncthreads();
+  mn = s.red[0];
+  mx = s.red[32];
+  for (int w = 1; w < WARPS; ++w) {
+    mn = min(mn, s.red[w]);
+    mx = max(mx, s.red[32 + w]);
+  }
+  const int vbits = (mn == mx) ? 0 : 64 - __clzll((long long)(mn ^ mx));
+  const int passes = (vbits + 7) / 8;
+  // Positions per thread for this bucket: warp w owns the contiguous run
+  // [w * 32 * ipt, (w + 1) * 32 * ipt), so ranks stay stable and no thread
+  // loops over the empty tail of a small bucket.
+  const int ipt = (int)((cnt + BS_THREADS - 1) / BS_THREADS);
+  const uint32_t wrun = (uint32_t)warp * 32u * (uint32_t)ipt;
+  int cur = 0;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = 8 * p;
+    for (int i = tid; i < WARPS * 256; i += BS_THREADS) (&s.hist[0][0])[i] = 0;
+    if (tid == 0) s.skip = 0;
+    __syncthreads();
+    // A. per-warp digit counts over this warp's run of positions.
+    uint32_t d[IPT];
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      d[j] = 256u;
+      if (j < ipt) {
+        const uint32_t pos = wrun + j * 32 + lane;
+        if (pos < cnt) d[j] = (uint32_t)(s.keys[s.idx[cur][pos]] >> shift) & 255u;
+        if (d[j] < 256u) atomicAdd(&s.hist[warp][d[j]], 1u);
+      }
+    }
+    __syncthreads();
+    // B. warp offsets per digit and digit bases: thread (digit dg, group g)
+    // scans warps 8g..8g+7 of its digit; the four group sums are combined per
+    // digit (scratch: the index array phase C writes, unused until then).
+    uint32_t* gs = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]);
+    const int dg = tid & 255, grp = tid >> 8;
+    uint32_t part = 0;
+#pragma unroll
+    for (int w = 8 * grp; w < 8 * grp + 8; ++w) {
+      const uint32_t c = s.hist[w][dg];
+      s.hist[w][dg] = part;
+      part += c;
+    }
+    gs[grp * 256 + dg] = part;
+    __syncthreads();
+    uint32_t count = 0;
+    if (tid < 256) {
+      count = gs[tid] + gs[256 + tid] + gs[512 + tid] + gs[768 + tid];
+      if (count == cnt) s.skip = 1;  // every key has this digit: the pass is the identity
+    }
+    uint32_t incl = 0;
+    if (tid < 256) {
+      incl = warp_inclusive_sum(count);
+      if (lane == 31) s.warp_sums[warp] = incl;
+    }
+    __syncthreads();
+    if (tid < 256) {
+      uint32_t pre = 0;
+      for (int w = 0; w < 8; ++w) pre += (w < warp) ? s.warp_sums[w] : 0u;
+      uint32_t run = pre + incl - count;  // digit base
+      for (int g = 0; g < 4; ++g) {
+        const uint32_t t = gs[g * 256 + tid];
+        gs[g * 256 + tid] = run;
+        run += t;
+      }
+    }
+    __syncthreads();
+    {
+      const uint32_t goff = gs[grp * 256 + dg];
+#pragma unroll
+      for (int w = 8 * grp; w < 8 * grp + 8; ++w) s.hist[w][dg] += goff;
+    }
+    __syncthreads();
+    if (s.skip) continue;  // block-uniform
+    // C. stable ranks (peer masks over valid lanes) and the scatter of indices.
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      if (j >= ipt || wrun + j * 32 >= cnt) break;  // warp-uniform
+      const uint32_t pos = wrun + j * 32 + lane;
+      const bool valid = d[j] < 256u;
+      uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+      for (int bit = 0; bit < 8; ++bit) {
+        const uint32_t x = (d[j] >> bit) & 1u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, x);
+        peers &= x ? bal : ~bal;
+      }
+      const int leader = valid ? 31 - __clz(peers) : 0;
+      uint32_t b0 = 0;
+      if (valid && lane == leader) b0 = atomicAdd(&s.hist[warp][d[j]], (uint32_t)__popc(peers));
+      b0 = __shfl_sync(0xffffffffu, b0, leader);
+      if (valid) s.idx[cur ^ 1][b0 + __popc(peers & lt_mask)] = s.idx[cur][pos];
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  // Runs of equal keys: order by original position (insertion sort; runs are
+  // short for Morton codes of distinct points, long runs take the fallback).
+  for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+    const uint64_t k = s.keys[s.idx[cur][i]];
+    if (i > 0 && s.keys[s.idx[cur][i - 1]] == k) continue;  // not a run start
+    uint32_t e = i + 1;
+    while (e < cnt && s.keys[s.idx[cur][e]] == k) ++e;
+    if (e - i > 1) {
+      if (e - i > (uint32_t)BS_MAX_RUN) {
+        atomicOr(flags, LFLAG_DUP_RUN);
+        continue;
+      }
+      for (uint32_t a = i + 1; a < e; ++a) {
+        const uint16_t x = s.idx[cur][a];
+        const uint32_t px = tpos[off + x];
+        uint32_t c = a;
+        while (c > i && tpos[off + s.idx[cur][c - 1]] > px) {
+          s.idx[cur][c] = s.idx[cur][c - 1];
+          --c;
+        }
+        s.idx[cur][c] = x;
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+    const uint16_t x = s.idx[cur][i];
+    out_keys[off + i] = s.keys[x];
+    out_vals[off + i] = tvals[off + x];
+  }
+  if (tid == 0) {
+    bmin[b] = mn;
+    bmax[b] = mx;
+  }
+}
+
+// Consecutive non-empty buckets must hold strictly increasing key ranges.
+__global__ void learned_order_check_kernel(const uint32_t* totals, const uint64_t* bmin, const uint64_t* bmax, int B,
+                                           uint32_t* flags) {
+  if (*flags) return;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+    if (totals[b] == 0) continue;
+    int nb = b + 1;
+    while (nb < B && totals[nb] == 0) ++nb;
+    if (nb < B && bmax[b] >= bmin[nb]) atomicOr(flags, LFLAG_ORDER);
+  }
+}
+
+// Fallback preparation: with any flag set, copy the input to the output.
+__global__ void cond_copy_kernel(const uint64_t* keys, const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out,
+                                 uint32_t n, const uint32_t* flags) {
+  if (*flags == 0) return;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    keys_out[i] = keys[i];
+    vals_out[i] = vals ? vals[i] : (uint32_t)i;
+  }
+}
+
+// Sum of per-tile histograms (diagnostic entry gtc_learned_histogram_u64).
+__global__ void sum_tiles_kernel(const uint32_t* c, uint32_t tiles, int B, uint32_t* out) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+    uint32_t t = 0;
+    for (uint32_t i = 0; i < tiles; ++i) t += c[(size_t)i * B + b];
+    out[b] = t;
+  }
+}
+
+// ------------------------------------------------------------ host side --
+struct LearnedWorkspace {
+  uint32_t* counts;   // [tiles][B]
+  uint32_t* totals;   // [B]
+  uint32_t* base;     // [B]
+  uint64_t* bmin;     // [B]
+  uint64_t* bmax;     // [B]
+  uint32_t* misc;     // [0] done counter
+  uint64_t* tkeys;    // [n]
+  uint32_t* tvals;    // [n]
+  uint32_t* tpos;     // [n]
+  void* sort_ws;      // onesweep fallback workspace
+};
+
+static size_t learned_ws_layout(uint32_t n, int B, LearnedWorkspace* W, char* p) {
+  const uint32_t tiles = ceil_div(n > 0 ? n : 1, LC_TILE);
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    char* q = p ? p + o : nullptr;
+    o += align_up(bytes, 256);
+    return q;
+  };
+  LearnedWorkspace w;
+  w.counts = reinterpret_cast<uint32_t*>(take((size_t)tiles * B * 4));
+  w.totals = reinterpret_cast<uint32_t*>(take((size_t)B * 4));
+  w.base = reinterpret_cast<uint32_t*>(take((size_t)B * 4));
+  w.bmin = reinterpret_cast<uint64_t*>(take((size_t)B * 8));
+  w.bmax = reinterpret_cast<uint64_t*>(take((size_t)B * 8));
+  w.misc = reinterpret_cast<uint32_t*>(take(256));
+  w.tkeys = reinterpret_cast<uint64_t*>(take((size_t)n * 8));
+  w.tvals = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  w.tpos = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  w.sort_ws = take(sort_workspace_bytes(n, 8, 0));
+  if (W) *W = w;
+  return o;
+}
+
+size_t learned_workspace_bytes(uint32_t n) { return learned_ws_layout(n, MAX_BUCKETS, nullptr, nullptr); }
+
+}  // namespace gtc
+
+using namespace gtc;
+
+struct gtc_learned_model {
+  int B = 0;
+  uint64_t* knots = nullptr;   // [B + 1]
+  float* heights = nullptr;    // [B + 1]
+  float* m1 = nullptr;         // Adam moments [B + 1]
+  float* m2 = nullptr;
+  float* grad = nullptr;       // [B + 1]
+  float* loss = nullptr;       // [1]
+  uint64_t* sample = nullptr;  // training sample
+  uint32_t sample_cap = 0;
+  uint32_t ns = 0;             // sample size of the last training call
+};
+
+namespace {
+gtc_status cuda_fail(gtc_ctx* ctx, const char* what, cudaError_t e) {
+  return context_error(ctx, e == cudaErrorMemoryAllocation ? GTC_ERR_OOM : GTC_ERR_CUDA, what, e);
+}
+#define LTRY(ctx, expr)                                  \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return cuda_fail(ctx, #expr, _e); \
+  } while (0)
+
+// Eytzinger knots + sorted knots + heights + per-bucket counters.
+size_t model_smem_bytes(int B) { return (size_t)B * 8 + (size_t)(B + 1) * 12 + (size_t)B * 4; }
+
+gtc_status prepare_sample(gtc_ctx* ctx, gtc_learned_model* m, const uint64_t* sorted, uint32_t n, uint32_t stride,
+                          cudaStream_t s) {
+  const uint32_t ns = (n + stride - 1) / stride;
+  if (ns < (uint32_t)m->B) return context_error(ctx, GTC_ERR_INVALID_ARG, "sample smaller than the bucket count", cudaSuccess);
+  if (m->sample_cap < ns) {
+    if (m->sample) cudaFree(m->sample);
+    m->sample = nullptr;
+    m->sample_cap = 0;
+    LTRY(ctx, cudaMalloc(&m->sample, (size_t)ns * 8));
+    m->sample_cap = ns;
+  }
+  m->ns = ns;
+  sample_kernel<<<min(ceil_div(ns, 256), 4096u), 256, 0, s>>>(sorted, ns, stride, m->sample);
+  LTRY(ctx, cudaGetLastError());
+  return GTC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learned_model** out) {
+  if (!ctx || !out) return GTC_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (buckets < 2 || buckets > MAX_BUCKETS || (buckets & (buckets - 1)))
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "buckets must be a power of two in [2, 8192]", cudaSuccess);
+  gtc_learned_model* m = new (std::nothrow) gtc_learned_model();
+  if (!m) return GTC_ERR_OOM;
+  m->B = buckets;
+  const size_t nb = (size_t)buckets + 1;
+  cudaError_t e = cudaMalloc(&m->knots, nb * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&m->heights, nb * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&m->m1, nb * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&m->m2, nb * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&m->grad, nb * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&m->loss, 256);
+  if (e != cudaSuccess) {
+    gtc_learned_model_destroy(m);
+    return cuda_fail(ctx, "allocating the learned model", e);
+  }
+  *out = m;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_model_destroy(gtc_learned_model* m) {
+  if (!m) return GTC_OK;
+  void* ptrs[] = {m->knots, m->heights, m->m1, m->m2, m->grad, m->loss, m->sample};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete m;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_model_params(gtc_learned_model* m, int* buckets, uint64_t** d_knots, float** d_heights) {
+  if (!m) return GTC_ERR_INVALID_ARG;
+  if (buckets) *buckets = m->B;
+  if (d_knots) *d_knots = m->knots;
+  if (d_heights) *d_heights = m->heights;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_model_export(gtc_learned_model* m, uint64_t* host_knots, float* host_heights) {
+  if (!m) return GTC_ERR_INVALID_ARG;
+  const size_t nb = (size_t)m->B + 1;
+  if (cudaDeviceSynchronize() != cudaSuccess) return GTC_ERR_CUDA;
+  if (host_knots && cudaMemcpy(host_knots, m->knots, nb * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return GTC_ERR_CUDA;
+  if (host_heights && cudaMemcpy(host_heights, m->heights, nb * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GTC_ERR_CUDA;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_train_u64(gtc_ctx* ctx, gtc_learned_model* m, const uint64_t* sorted_keys, uint32_t n,
+                                         uint32_t sample_stride, int iters, float lr, float* d_loss,
+                                         gtc_stream_t stream) {
+  if (!ctx || !m || !sorted_keys || sample_stride == 0 || iters < 0) return GTC_ERR_INVALID_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  gtc_status st = prepare_sample(ctx, m, sorted_keys, n, sample_stride, s);
+  if (st != GTC_OK) return st;
+  const int B = m->B;
+  knots_init_kernel<<<ceil_div(B + 1, 256), 256, 0, s>>>(m->sample, m->ns, B, m->knots, m->heights, m->m1, m->m2);
+  LTRY(ctx, cudaGetLastError());
+  for (int it = 1; it <= iters; ++it) {
+    grad_kernel<<<ceil_div(B + 1, 128), 128, 0, s>>>(m->sample, m->ns, m->knots, m->heights, B, m->grad);
+    adam_kernel<<<1, 1024, 0, s>>>(m->heights, m->grad, m->m1, m->m2, B, lr, it);
+  }
+  LTRY(ctx, cudaGetLastError());
+  LTRY(ctx, cudaMemsetAsync(m->loss, 0, 4, s));
+  loss_kernel<<<min(ceil_div(m->ns, 256), 1024u), 256, 0, s>>>(m->sample, m->ns, m->knots, m->heights, B, m->loss);
+  LTRY(ctx, cudaGetLastError());
+  if (d_loss) LTRY(ctx, cudaMemcpyAsync(d_loss, m->loss, 4, cudaMemcpyDeviceToDevice, s));
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_gradient_u64(gtc_ctx* ctx, gtc_learned_model* m, const uint64_t* sorted_keys, uint32_t n,
+                                            uint32_t sample_stride, int init, float* d_grad, float* d_loss,
+                                            gtc_stream_t stream) {
+  if (!ctx || !m || !sorted_keys || sample_stride == 0 || !d_grad) return GTC_ERR_INVALID_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  gtc_status st = prepare_sample(ctx, m, sorted_keys, n, sample_stride, s);
+  if (st != GTC_OK) return st;
+  const int B = m->B;
+  if (init)
+    knots_init_kernel<<<ceil_div(B + 1, 256), 256, 0, s>>>(m->sample, m->ns, B, m->knots, m->heights, m->m1, m->m2);
+  grad_kernel<<<ceil_div(B + 1, 128), 128, 0, s>>>(m->sample, m->ns, m->knots, m->heights, B, d_grad);
+  if (d_loss) {
+    LTRY(ctx, cudaMemsetAsync(d_loss, 0, 4, s));
+    loss_kernel<<<min(ceil_div(m->ns, 256), 1024u), 256, 0, s>>>(m->sample, m->ns, m->knots, m->heights, B, d_loss);
+  }
+  LTRY(ctx, cudaGetLastError());
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys,
+                                             uint32_t n, uint32_t* d_counts, gtc_stream_t stream) {
+  if (!ctx || !m || !d_counts || (n && !keys)) return GTC_ERR_INVALID_ARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int B = m->B;
+  const uint32_t tiles = ceil_div(n > 0 ? n : 1, LC_TILE);
+  uint32_t* counts = nullptr;
+  LTRY(ctx, cudaMallocAsync(reinterpret_cast<void**>(&counts), (size_t)tiles * B * 4, s));
+  const size_t smem = model_smem_bytes(B);
+  LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)model_smem_bytes(MAX_BUCKETS)));
+  learned_count_kernel<<<tiles, LC_THREADS, smem, s>>>(keys, n, m->knots, m->heights, B, counts);
+  LTRY(ctx, cudaGetLastError());
+  sum_tiles_kernel<<<ceil_div(B, 256), 256, 0, s>>>(counts, tiles, B, d_counts);
+  LTRY(ctx, cudaGetLastError());
+  LTRY(ctx, cudaFreeAsync(counts, s));
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys,
+                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
+                                        void* ws, size_t ws_bytes, uint32_t* d_flags, gtc_stream_t stream) {
+  if (!ctx || !m || !d_flags) return GTC_ERR_INVALID_ARG;
+  if (n >= (1u << 30)) return context_error(ctx, GTC_ERR_INVALID_ARG, "n must be < 2^30", cudaSuccess);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  LTRY(ctx, cudaMemsetAsync(d_flags, 0, 4, s));
+  if (n == 0) return GTC_OK;
+  if (!keys || !keys_out || !vals_out)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "keys, keys_out and vals_out are required", cudaSuccess);
+  if (keys == keys_out || (vals && vals == vals_out))
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "the learned sort is out of place", cudaSuccess);
+  const int B = m->B;
+  const size_t need = learned_ws_layout(n, B, nullptr, nullptr);
+  if (!ws || ws_bytes < need || (reinterpret_cast<uintptr_t>(ws) & 255))
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "learned sort workspace missing, too small or unaligned",
+                         cudaSuccess);
+  LearnedWorkspace W;
+  learned_ws_layout(n, B, &W, reinterpret_cast<char*>(ws));
+  const uint32_t tiles = ceil_div(n, LC_TILE);
+  const size_t msmem = model_smem_bytes(B);
+  static bool attr = false;
+  if (!attr) {
+    LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)model_smem_bytes(MAX_BUCKETS)));
+    LTRY(ctx, cudaFuncSetAttribute(learned_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)model_smem_bytes(MAX_BUCKETS)));
+    LTRY(ctx, cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(BucketSmem)));
+    attr = true;
+  }
+  LTRY(ctx, cudaMemsetAsync(W.misc, 0, 256, s));
+  learned_count_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, n, m->knots, m->heights, B, W.counts);
+  learned_scan_kernel<<<ceil_div(B, 1024), 1024, 0, s>>>(W.counts, tiles, B, m->heights, W.totals, W.base, d_flags,
+                                                        W.misc);
+  learned_scatter_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, vals, n, m->knots, m->heights, B, W.counts, W.base,
+                                                         W.tkeys, W.tvals, W.tpos, d_flags);
+  bucket_sort_kernel<<<B, BS_THREADS, sizeof(BucketSmem), s>>>(W.tkeys, W.tvals, W.tpos, W.base, W.totals, keys_out,
+                                                               vals_out, W.bmin, W.bmax, d_flags);
+  learned_order_check_kernel<<<ceil_div(B, 256), 256, 0, s>>>(W.totals, W.bmin, W.bmax, B, d_flags);
+  LTRY(ctx, cudaGetLastError());
+  // Fallback: copy + plain onesweep, all gated on the flag word.
+  cond_copy_kernel<<<context_launch(ctx, stream).num_sms * 8, 256, 0, s>>>(keys, vals, keys_out, vals_out, n, d_flags);
+  Launch L = context_launch(ctx, stream);
+  L.run_if = d_flags;
+  const SortWorkspace SW = carve_sort_workspace(W.sort_ws, n, 8, 0);
+  LTRY(ctx, cudaMemsetAsync(SW.header, 0, SW.header_words * 4, s));
+  LTRY(ctx, launch_global_hist<uint64_t>(L, keys_out, n, 0, 64, SW, 8));
+  bool in_alt = false;
+  LTRY(ctx, launch_onesweep_passes<uint64_t>(L, keys_out, vals_out, W.tkeys, W.tvals, n, 0, 64, SW, 8, &in_alt,
+                                             nullptr));
+  return GTC_OK;
+}
+
+}  // extern "C"

@@ -26,7 +26,6 @@
 namespace gtc {
 
 constexpr int OCT_THREADS = 256;
-constexpr int OCT_CAP = 512;  // nodes staged per block pass (32 KB of shared memory)
 
 template <class K>
 __device__ __forceinline__ K level_prefix(K code, int level) {  // top 3*level bits, kept in place
@@ -53,7 +52,8 @@ __device__ __forceinline__ void set_child(int4& lo, int4& hi, int w, int32_t v) 
   hi.w = (w == 7) ? v : hi.w;
 }
 
-// Writes one 64-byte node, into the block's staging area or straight to HBM.
+// Writes one 64-byte node (four 16-byte stores), straight to HBM or into a
+// staging area.
 struct NodeSink {
   int4* stage;
   gtc_octnode* nodes;

@@ -103,7 +103,9 @@ template <class K, int THREADS>
 __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restrict__ keys, uint32_t n, int begin_bit,
                                                               int end_bit, int passes, uint32_t* counts,
                                                               uint32_t* bin_offsets, uint32_t* done,
-                                                              uint32_t* zero_ptr, size_t zero_words) {
+                                                              uint32_t* zero_ptr, size_t zero_words,
+                                                              const uint32_t* run_if) {
+  if (run_if && *run_if == 0) return;
   __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
   __shared__ uint32_t s_warp_sums[8];
   __shared__ uint32_t s_last;
@@ -171,7 +173,9 @@ __global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__
                                                            const uint32_t* __restrict__ bin_off,
                                                            uint32_t* __restrict__ desc,
                                                            uint32_t* __restrict__ tile_counter,
-                                                           uint32_t* __restrict__ status) {
+                                                           uint32_t* __restrict__ status,
+                                                           const uint32_t* run_if) {
+  if (run_if && *run_if == 0) return;
   using S = OnesweepSmem<K, THREADS, KPT>;
   constexpr int WARPS = S::WARPS;
   constexpr int TILE = S::TILE;
@@ -329,7 +333,9 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tm
                                                                uint32_t dmask, const uint32_t* __restrict__ bin_off,
                                                                uint32_t* __restrict__ desc,
                                                                uint32_t* __restrict__ tile_counter,
-                                                               uint32_t* __restrict__ status) {
+                                                               uint32_t* __restrict__ status,
+                                                               const uint32_t* run_if) {
+  if (run_if && *run_if == 0) return;
   using S = TmaSmem<K, THREADS, KPT, HV>;
   constexpr int TILE = S::TILE;
   constexpr int WARPS = S::WARPS;
@@ -508,7 +514,7 @@ static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin
   }
   const uint32_t tiles = ceil_div(n, S::TILE);
   kern<<<tiles, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
-                                                L.status);
+                                                L.status, L.run_if);
   return cudaGetLastError();
 }
 
@@ -530,7 +536,7 @@ static cudaError_t launch_tma(const Launch& L, const K* kin, const uint32_t* vin
   const uint32_t tiles = ceil_div(n, S::TILE);
   const uint32_t grid = min(tiles, (uint32_t)(per_sm * L.num_sms));
   kern<<<grid, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
-                                               L.status);
+                                               L.status, L.run_if);
   return cudaGetLastError();
 }
 
@@ -605,7 +611,7 @@ cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int b
   const uint32_t want = ceil_div(n, T * 16);
   const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 2));
   global_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(keys, n, begin_bit, end_bit, passes, W.counts, W.bin_offsets,
-                                                     W.header, W.desc, W.desc_words);
+                                                     W.header, W.desc, W.desc_words, L.run_if);
   return cudaGetLastError();
 }
 template cudaError_t launch_global_hist<uint32_t>(const Launch&, const uint32_t*, uint32_t, int, int,

@@ -307,6 +307,86 @@ class OctreePlan:
                             self.left[:m], self.parent[:m], self.edge[:m], self.ps[:u], self.nodes[:o], u, m, o)
 
 
+OP_LEARNED_SORT = 6
+LEARNED_FLAGS = {1: "overflow", 2: "order", 4: "non-monotone model", 8: "long run of equal keys"}
+
+
+class LearnedModel:
+    """Learned-bucket CDF model (gtc_learned_model_*): piecewise linear with
+    `buckets` segments, trained on the GPU from a sample of sorted keys."""
+
+    def __init__(self, ctx: Context, buckets: int):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx.check(ctx.L.gtc_learned_model_create(ctx.h, buckets, ctypes.byref(h)))
+        self.h = h
+        self.buckets = buckets
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.gtc_learned_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        """(knots u64[B+1], heights f32[B+1]) as host numpy arrays."""
+        kn = np.zeros(self.buckets + 1, np.uint64)
+        hy = np.zeros(self.buckets + 1, np.float32)
+        self.ctx.check(self.ctx.L.gtc_learned_model_export(self.h, kn.ctypes.data_as(ctypes.c_void_p),
+                                                           hy.ctypes.data_as(ctypes.c_void_p)))
+        return kn, hy
+
+    def train(self, sorted_keys, stride: int = 100, iters: int = 100, lr: float = 1e-4) -> float:
+        torch = _torch()
+        loss = torch.zeros(1, dtype=torch.float32, device=sorted_keys.device)
+        self.ctx.check(self.ctx.L.gtc_learned_train_u64(self.ctx.h, self.h, _ptr(sorted_keys), sorted_keys.numel(),
+                                                        stride, iters, lr, _ptr(loss), _stream()))
+        return float(loss.item())
+
+    def gradient(self, sorted_keys, stride: int = 100, init: bool = True):
+        torch = _torch()
+        g = torch.zeros(self.buckets + 1, dtype=torch.float32, device=sorted_keys.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=sorted_keys.device)
+        self.ctx.check(self.ctx.L.gtc_learned_gradient_u64(self.ctx.h, self.h, _ptr(sorted_keys),
+                                                           sorted_keys.numel(), stride, 1 if init else 0, _ptr(g),
+                                                           _ptr(loss), _stream()))
+        return g, float(loss.item())
+
+    def histogram(self, keys):
+        torch = _torch()
+        c = torch.zeros(self.buckets, dtype=torch.int32, device=keys.device)
+        self.ctx.check(self.ctx.L.gtc_learned_histogram_u64(self.ctx.h, self.h, _ptr(keys), keys.numel(), _ptr(c),
+                                                            _stream()))
+        return c
+
+    def sort(self, keys, vals=None, ws=None, keys_out=None, vals_out=None):
+        """Out-of-place learned sort; returns (keys_out, vals_out, flags tensor)."""
+        torch = _torch()
+        n = keys.numel()
+        keys_out = torch.empty_like(keys) if keys_out is None else keys_out
+        vals_out = torch.empty(n, dtype=torch.int32, device=keys.device) if vals_out is None else vals_out
+        ws = self.ctx.workspace(OP_LEARNED_SORT, n, 64) if ws is None else ws
+        flags = torch.zeros(1, dtype=torch.int32, device=keys.device)
+        self.ctx.check(self.ctx.L.gtc_learned_sort_u64(self.ctx.h, self.h, _ptr(keys), _ptr(vals), _ptr(keys_out),
+                                                       _ptr(vals_out), n, _ptr(ws), ws.numel(), _ptr(flags), _stream()))
+        return keys_out, vals_out, flags
+
+
+def learned_buckets_for(n: int) -> int:
+    """Bucket count for n keys: 2^12, raised to the next power of two while the
+    average bucket would exceed 8192 keys (the on-chip bucket sort holds at
+    most 16384), capped at 8192."""
+    b = 4096
+    while n / b > 8192 and b < 8192:
+        b *= 2
+    return b
+
+
 def build_octree(ctx: Context, pts, key_bits: int, min_coord=0.0, rng=1024.0) -> OctreeResult:
     plan = OctreePlan(ctx, pts.shape[0], key_bits)
     plan.launch(pts, min_coord=min_coord, rng=rng)

@@ -56,6 +56,14 @@ SIGNATURES = {
     "gtc_host_alloc": (st, [ctypes.POINTER(P), sz]),
     "gtc_host_free": (st, [P]),
     "gtc_sort_pairs_u32_noalloc": (st, [P, P, P, P, P, u32, i_, i_, P]),
+    "gtc_learned_model_create": (st, [P, i_, ctypes.POINTER(P)]),
+    "gtc_learned_model_destroy": (st, [P]),
+    "gtc_learned_model_params": (st, [P, ctypes.POINTER(i_), ctypes.POINTER(P), ctypes.POINTER(P)]),
+    "gtc_learned_model_export": (st, [P, P, P]),
+    "gtc_learned_train_u64": (st, [P, P, P, u32, u32, i_, f32, P, P]),
+    "gtc_learned_gradient_u64": (st, [P, P, P, u32, u32, i_, P, P, P]),
+    "gtc_learned_histogram_u64": (st, [P, P, P, u32, P, P]),
+    "gtc_learned_sort_u64": (st, [P, P, P, P, P, P, u32, P, sz, P, P]),
     "gtc_sort_num_variants": (i_, []),
     "gtc_sort_variant_shape": (st, [i_, ctypes.POINTER(i_), ctypes.POINTER(i_)]),
     "gtc_sort_set_variant": (st, [i_, i_]),

@@ -100,7 +100,8 @@ typedef enum gtc_op {
   GTC_OP_UNIQUE = 2,
   GTC_OP_PARTIAL_SUM = 3,
   GTC_OP_BUILD_OCTREE = 4,
-  GTC_OP_GLOBAL_HISTOGRAM = 5
+  GTC_OP_GLOBAL_HISTOGRAM = 5,
+  GTC_OP_LEARNED_SORT = 6
 } gtc_op;
 /* Bytes of device workspace `op` needs for n elements of key_bits-wide keys.
  * Workspace pointers must be 256-byte aligned. */
@@ -265,6 +266,53 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
 GTC_API gtc_status gtc_sort_pairs_u32_noalloc(gtc_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t* keys_alt,
                                               uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
                                               gtc_stream_t stream);
+
+/* ------------------------------------------------ learned-bucket sort --- */
+/* No counterpart in the reference: a learned stand-in for the top radix
+ * passes of the 64-bit sort, whose output is defined to be exactly the stable
+ * onesweep result (gtc_sort_pairs_u64 on bits [0, 64)).
+ *
+ * The model is a piecewise-linear CDF with `buckets` segments (a power of two
+ * <= 8192): knots at quantiles of a sample of previously sorted keys, FP32
+ * heights trained on the GPU (forward / backward / Adam kernels, mean squared
+ * error against the sample's empirical CDF).  gtc_learned_sort_u64 scatters
+ * the keys into `buckets` buckets in one pass, sorts each bucket on chip, and
+ * checks on the device that no bucket overflowed its on-chip capacity (16384
+ * keys) and that bucket key ranges are ordered.  If a check fails the flag
+ * word *d_flags is nonzero and the plain onesweep, launched in the same stream
+ * and gated on that word, produces the result instead (bits: 1 overflow,
+ * 2 order, 4 non-monotone model, 8 long run of equal keys). */
+typedef struct gtc_learned_model gtc_learned_model;
+GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learned_model** out);
+GTC_API gtc_status gtc_learned_model_destroy(gtc_learned_model* model);
+/* Device pointers of the model's knots (u64[buckets + 1]) and heights
+ * (f32[buckets + 1]). */
+GTC_API gtc_status gtc_learned_model_params(gtc_learned_model* model, int* buckets, uint64_t** d_knots,
+                                            float** d_heights);
+/* Synchronous copy of the knots and heights to host arrays of buckets + 1. */
+GTC_API gtc_status gtc_learned_model_export(gtc_learned_model* model, uint64_t* host_knots, float* host_heights);
+/* Samples every sample_stride-th key of `sorted_keys` (a previous sort's
+ * output), places the knots at the sample's quantiles and runs `iters` Adam
+ * steps of learning rate lr on the heights.  *d_loss (device, nullable)
+ * receives the final mean squared error. */
+GTC_API gtc_status gtc_learned_train_u64(gtc_ctx* ctx, gtc_learned_model* model, const uint64_t* sorted_keys,
+                                         uint32_t n, uint32_t sample_stride, int iters, float lr, float* d_loss,
+                                         gtc_stream_t stream);
+/* Gradient (d_grad: f32[buckets + 1]) and loss of the current heights on the
+ * sample of sorted_keys (init != 0 first resets knots and heights): the
+ * backward kernel the training uses, exposed for gradient checks. */
+GTC_API gtc_status gtc_learned_gradient_u64(gtc_ctx* ctx, gtc_learned_model* model, const uint64_t* sorted_keys,
+                                            uint32_t n, uint32_t sample_stride, int init, float* d_grad,
+                                            float* d_loss, gtc_stream_t stream);
+/* Bucket occupancy of `keys` under the model (d_counts: u32[buckets]). */
+GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_model* model, const uint64_t* keys,
+                                             uint32_t n, uint32_t* d_counts, gtc_stream_t stream);
+/* Out-of-place sort of (keys, vals) into (keys_out, vals_out); vals may be
+ * NULL (the payload is then the input index).  Workspace:
+ * gtc_workspace_size(GTC_OP_LEARNED_SORT, n, 64). */
+GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* model, const uint64_t* keys,
+                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
+                                        void* ws, size_t ws_bytes, uint32_t* d_flags, gtc_stream_t stream);
 
 /* ------------------------------------------------------ sort variants --- */
 /* Onesweep tile shapes compiled into the library (threads per block and keys

@@ -76,6 +76,8 @@ def lib():
             "orc_validate_octree": (i_, [P, u32, u32, f32]),
             "orc_build_octree": (i_, [P, u32, f32, f32, i_, P, P, P, P, P, P, P, P, P, P, P, u32, i_, P]),
             "orc_max_threads": (i_, []),
+            "orc_pwl_loss_grad": (ctypes.c_double, [P, u32, P, P, i_, P]),
+            "orc_pwl_buckets": (None, [P, u32, P, P, i_, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -236,3 +238,23 @@ def build_octree(pts: np.ndarray, key_bits: int, min_coord=0.0, rng=1024.0, flag
     times = dict(zip(STAGES, stage_ms[:7].tolist()))
     times["total"] = total_ms
     return out, times
+
+
+def pwl_loss_grad(sample: np.ndarray, knots: np.ndarray, heights: np.ndarray):
+    """Loss and gradient of the learned-bucket CDF model (double precision)."""
+    sample = np.ascontiguousarray(sample, dtype=np.uint64)
+    knots = np.ascontiguousarray(knots, dtype=np.uint64)
+    heights = np.ascontiguousarray(heights, dtype=np.float32)
+    B = knots.size - 1
+    grad = np.zeros(B + 1, np.float64)
+    loss = lib().orc_pwl_loss_grad(_p(sample), sample.size, _p(knots), _p(heights), B, _p(grad))
+    return float(loss), grad
+
+
+def pwl_buckets(keys: np.ndarray, knots: np.ndarray, heights: np.ndarray) -> np.ndarray:
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    knots = np.ascontiguousarray(knots, dtype=np.uint64)
+    heights = np.ascontiguousarray(heights, dtype=np.float32)
+    out = np.zeros(keys.size, np.uint32)
+    lib().orc_pwl_buckets(_p(keys), keys.size, _p(knots), _p(heights), knots.size - 1, _p(out))
+    return out

@@ -588,6 +588,44 @@ int orc_build_octree(const float* pts, uint32_t n, float mn, float rg, int key_b
   return -1;
 }
 
+static int pwl_segment(uint64_t key, const uint64_t* kn, int B) {
+  int lo = 0, hi = B;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (kn[mid] <= key) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+double orc_pwl_loss_grad(const uint64_t* s, uint32_t ns, const uint64_t* kn, const float* y, int B, double* grad) {
+  for (int k = 0; k <= B; ++k) grad[k] = 0.0;
+  double loss = 0.0;
+  for (uint32_t j = 0; j < ns; ++j) {
+    const int seg = pwl_segment(s[j], kn, B);
+    const uint64_t k0 = kn[seg], k1 = kn[seg + 1];
+    const double w = (k1 > k0) ? (double)(s[j] - k0) / (double)(k1 - k0) : 0.0;
+    const double F = (double)y[seg] + ((double)y[seg + 1] - (double)y[seg]) * w;
+    const double r = F - ((double)j + 0.5) / (double)ns;
+    loss += r * r;
+    grad[seg] += 2.0 * r * (1.0 - w) / ns;
+    grad[seg + 1] += 2.0 * r * w / ns;
+  }
+  return loss / ns;
+}
+
+void orc_pwl_buckets(const uint64_t* keys, uint32_t n, const uint64_t* kn, const float* y, int B, uint32_t* out) {
+  for (uint32_t i = 0; i < n; ++i) {
+    const int seg = pwl_segment(keys[i], kn, B);
+    const uint64_t k0 = kn[seg], k1 = kn[seg + 1];
+    const double w = (k1 > k0) ? (double)(keys[i] - k0) / (double)(k1 - k0) : 0.0;
+    double F = (double)y[seg] + ((double)y[seg + 1] - (double)y[seg]) * w;
+    F = std::min(std::max(F, (double)y[seg]), (double)y[seg + 1]);
+    long b = (long)(F * B);
+    out[i] = (uint32_t)std::min<long>(std::max<long>(b, 0), B - 1);
+  }
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -146,6 +146,17 @@ int orc_build_octree(const float* pts, uint32_t n, float min_coord, float range,
 
 int orc_max_threads(void);
 
+/* Learned-bucket model (no reference counterpart): loss and gradient of the
+ * piecewise-linear CDF with knots kn[0..B] and heights y[0..B] on a sorted
+ * sample s[0..ns): L = mean_j (F(s_j) - (j + 0.5)/ns)^2, F linear inside
+ * segment [kn[k], kn[k+1]) (the segment of a key is the last knot <= key).
+ * Double precision; the checker of the GPU backward kernel. */
+double orc_pwl_loss_grad(const uint64_t* sample, uint32_t ns, const uint64_t* kn, const float* y, int B,
+                         double* grad);
+/* Bucket of each key under the model: floor(B * F), F clamped to the
+ * segment's end heights, in double precision. */
+void orc_pwl_buckets(const uint64_t* keys, uint32_t n, const uint64_t* kn, const float* y, int B, uint32_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,134 @@
+"""Learned-bucket sort (gtc_learned_*): GPU training gradients against the
+oracle, output bit-exact against the stable sort, fallback on a shifted
+distribution, and the gain of the trained model over equal-width top-bit
+bucketing."""
+import numpy as np
+import pytest
+
+from gtc import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _keys(oracle, n, seed, shifted=False):
+    return oracle.morton(W.config5_points(n, seed=seed, shifted=shifted), 64)
+
+
+def _dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).cuda()
+
+
+def _trained(ctx, oracle, gtc_mod, n_prior=2_000_000, buckets=1024, iters=50):
+    prior = np.sort(_keys(oracle, n_prior, seed=1))
+    model = gtc_mod.LearnedModel(ctx, buckets)
+    model.train(_dev(prior), stride=100, iters=iters, lr=1e-4)
+    return model, prior
+
+
+def test_gradient_matches_oracle(ctx, oracle, gtc_mod):
+    prior = np.sort(_keys(oracle, 1_000_000, seed=1))
+    model = gtc_mod.LearnedModel(ctx, 512)
+    sample = prior[::100]
+    for init in (True, False):
+        g, loss = model.gradient(_dev(prior), stride=100, init=init)
+        kn, hy = model.params()
+        eloss, eg = oracle.pwl_loss_grad(sample, kn, hy)
+        got = g.cpu().numpy().astype(np.float64)
+        scale = np.abs(eg).max()
+        assert np.allclose(got, eg, rtol=2e-3, atol=2e-3 * scale), (init, np.abs(got - eg).max(), scale)
+        assert abs(loss - eloss) <= 1e-3 * max(eloss, 1e-12) + 1e-9
+        if init:
+            model.train(_dev(prior), stride=100, iters=20, lr=1e-4)
+
+
+def test_training_reduces_loss_and_keeps_monotone(ctx, oracle, gtc_mod):
+    prior = np.sort(_keys(oracle, 1_000_000, seed=1))
+    model = gtc_mod.LearnedModel(ctx, 512)
+    _, loss0 = model.gradient(_dev(prior), stride=100, init=True)
+    loss1 = model.train(_dev(prior), stride=100, iters=200, lr=1e-4)
+    assert loss1 < loss0
+    kn, hy = model.params()
+    assert np.all(np.diff(hy) >= 0) and hy[0] == 0 and hy[-1] == 1
+    assert np.all(np.diff(kn.astype(np.float64)) >= 0)
+
+
+def test_buckets_match_oracle(ctx, oracle, gtc_mod):
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=1024, iters=30)
+    keys = _keys(oracle, 300_000, seed=2)
+    kn, hy = model.params()
+    exp = np.bincount(oracle.pwl_buckets(keys, kn, hy), minlength=1024)
+    got = model.histogram(_dev(keys)).cpu().numpy()
+    # float vs double interpolation may move a key sitting on a bucket edge
+    assert np.abs(got.astype(np.int64) - exp).sum() <= 4
+    assert got.sum() == keys.size
+
+
+@pytest.mark.parametrize("n", [1, 1000, 777_777, 4_000_000])
+def test_learned_sort_bit_exact(ctx, oracle, gtc_mod, n):
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=1024 if n < 4_000_000 else 4096)
+    keys = _keys(oracle, n, seed=2)
+    vals = np.arange(n, dtype=np.uint32)[::-1].copy()  # a payload that is not the index
+    import torch
+
+    tv = torch.from_numpy(vals.view(np.int32)).cuda()
+    ko, vo, flags = model.sort(_dev(keys), tv)
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
+    assert np.array_equal(vo.cpu().numpy().view(np.uint32), vals[order])
+    ctx.device_status()
+    if n >= 1000:
+        assert int(flags.item()) == 0, gtc_mod.LEARNED_FLAGS
+
+
+def test_learned_matches_onesweep(ctx, oracle, gtc_mod):
+    import torch
+
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=4096)
+    keys = _dev(_keys(oracle, 6_000_000, seed=3))
+    ko, vo, flags = model.sort(keys)
+    k2, v2 = keys.clone(), torch.arange(keys.numel(), dtype=torch.int32, device="cuda")
+    ctx.sort_pairs(k2, v2, 0, 64)
+    assert int(flags.item()) == 0
+    assert torch.equal(ko, k2) and torch.equal(vo, v2)
+
+
+def test_shifted_distribution_falls_back(ctx, oracle, gtc_mod):
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=1024)
+    keys = _keys(oracle, 3_000_000, seed=4, shifted=True)
+    ko, vo, flags = model.sort(_dev(keys))
+    assert int(flags.item()) & 1  # overflow: the model does not fit the shifted mixture
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
+    assert np.array_equal(vo.cpu().numpy().view(np.uint32), order.astype(np.uint32))
+
+
+def test_duplicates_and_equal_keys(ctx, oracle, gtc_mod):
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=1024)
+    base = _keys(oracle, 200_000, seed=5)
+    rng = np.random.default_rng(0)
+    dup = np.concatenate([base, base[rng.integers(0, base.size, 50_000)]])  # short runs of equal keys
+    rng.shuffle(dup)
+    same = np.full(100_000, base[17], np.uint64)  # one long run: falls back, still exact
+    for keys, must_fall_back in ((dup, False), (same, True)):
+        ko, vo, flags = model.sort(_dev(keys))
+        order = np.argsort(keys, kind="stable")
+        assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
+        assert np.array_equal(vo.cpu().numpy().view(np.uint32), order.astype(np.uint32))
+        assert (int(flags.item()) != 0) == must_fall_back
+
+
+def test_trained_model_gain_over_top_bits(ctx, oracle, gtc_mod):
+    """What the trained CDF model buys: bucket balance.  Equal-width top-bit
+    bucketing of the same clustered Morton keys piles a large share into a few
+    buckets (which would overflow the on-chip bucket sort); the model keeps
+    every bucket near the mean."""
+    model, _ = _trained(ctx, oracle, gtc_mod, n_prior=4_000_000, buckets=4096, iters=100)
+    keys = _keys(oracle, 4_000_000, seed=2)
+    learned = model.histogram(_dev(keys)).cpu().numpy()
+    top = np.bincount((keys >> np.uint64(52)).astype(np.int64), minlength=4096)
+    mean = keys.size / 4096
+    assert learned.max() / mean < 2.0
+    assert top.max() / mean > 20.0
+    assert (top.max() / mean) / (learned.max() / mean) > 10.0

@@ -170,6 +170,30 @@ def test_eight_corner_cells(oracle):
     assert sorted(out["nodes"][0]["children"].tolist()) == list(range(8))
 
 
+def test_pwl_gradient_finite_differences(oracle):
+    """The learned-model gradient of the oracle (the checker of the GPU
+    backward kernel) agrees with central finite differences of its loss."""
+    rng = np.random.default_rng(3)
+    sample = np.sort(rng.integers(0, 1 << 62, size=5000, dtype=np.uint64))
+    B = 16
+    q = (np.arange(B + 1) * (sample.size - 1) // B)
+    kn = sample[q].copy()
+    kn[0] = 0
+    kn[-1] = np.uint64(2**64 - 1)
+    y = np.sort(rng.random(B + 1).astype(np.float32))
+    loss, g = oracle.pwl_loss_grad(sample, kn, y)
+    for k in range(B + 1):
+        h = 1e-3
+        yp, ym = y.astype(np.float64).copy(), y.astype(np.float64).copy()
+        yp[k] += h
+        ym[k] -= h
+        lp, _ = oracle.pwl_loss_grad(sample, kn, yp.astype(np.float32))
+        lm, _ = oracle.pwl_loss_grad(sample, kn, ym.astype(np.float32))
+        # float32 heights: the perturbation is representable to ~1e-7 relative
+        fd = (lp - lm) / (np.float32(y[k] + h) - np.float32(y[k] - h))
+        assert abs(fd - g[k]) <= 1e-3 * max(abs(g[k]), 1e-3), (k, fd, g[k])
+
+
 @pytest.mark.parametrize("key_bits", [32, 64])
 def test_oracle_matches_committed_vectors(oracle, key_bits):
     g = np.load(os.path.join(GOLDEN, f"oracle_small_{key_bits}.npz"))
