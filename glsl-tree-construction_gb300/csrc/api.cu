@@ -375,6 +375,18 @@ namespace gtc {
 // Accessors for entry points defined in other translation units.
 Launch context_launch(gtc_ctx* ctx, gtc_stream_t stream) { return launch_of(ctx, stream); }
 gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_t e) { return fail(ctx, s, msg, e); }
+cudaEvent_t context_stage_begin(gtc_ctx* ctx, gtc_stream_t stream) {
+  if (!ctx->profiling) return nullptr;
+  cudaEvent_t a = get_event(ctx);
+  cudaEventRecord(a, S(stream));
+  return a;
+}
+void context_stage_end(gtc_ctx* ctx, gtc_stream_t stream, cudaEvent_t a, int stage) {
+  if (!a) return;
+  cudaEvent_t b = get_event(ctx);
+  cudaEventRecord(b, S(stream));
+  ctx->pending.push_back({a, b, stage});
+}
 }  // namespace gtc
 
 // =================================================================== C ABI ==
@@ -445,6 +457,7 @@ GTC_API gtc_status gtc_device_status(gtc_ctx* ctx, gtc_stream_t stream) {
   GTC_TRY(ctx, cudaMemset(ctx->d_status, 0, 4));
   if (word & DEV_TIMEOUT) return fail(ctx, GTC_ERR_TIMEOUT, "a look-back wait ran out of its poll budget");
   if (word & DEV_CAPACITY) return fail(ctx, GTC_ERR_CAPACITY, "octree node buffer too small");
+  if (word & DEV_BAD_INPUT) return fail(ctx, GTC_ERR_INVALID_ARG, "device-resident offsets are not a valid partition");
   if (word & DEV_INTERNAL) return fail(ctx, GTC_ERR_CUDA, "device consistency check failed");
   return GTC_OK;
 }

@@ -12,6 +12,7 @@ namespace gtc {
 constexpr uint32_t DEV_TIMEOUT = 1u;   // a bounded spin ran out
 constexpr uint32_t DEV_CAPACITY = 2u;  // an output buffer was too small
 constexpr uint32_t DEV_INTERNAL = 4u;  // an impossible state was detected
+constexpr uint32_t DEV_BAD_INPUT = 8u;  // device-resident arguments failed their checks
 
 // Descriptor flags for decoupled look-back: value << 2 | flag.
 constexpr uint32_t FLAG_NOT_READY = 0u;
@@ -288,6 +289,9 @@ template <class K>
 cudaError_t launch_unique(const Launch& L, const K* keys_in, const uint32_t* vals_in, K* keys_out,
                           uint32_t* vals_out, uint32_t n, uint32_t* d_count, void* ws);
 cudaError_t launch_inclusive_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t n, void* ws);
+// Inclusive scan of *d_count (<= n_max) elements, the count read on the device.
+cudaError_t launch_inclusive_scan_dev(const Launch& L, const uint32_t* in, uint32_t* out, const uint32_t* d_count,
+                                      uint32_t n_max, void* ws);
 // Node offsets over u = m + 1 entries, m = (d_u ? *d_u - 1 : m_host).
 cudaError_t launch_node_offsets(const Launch& L, const uint32_t* edge, uint32_t* ps, const uint32_t* d_u,
                                 uint32_t m_host, uint32_t n_max, uint32_t* d_o, void* ws);

@@ -8,7 +8,7 @@
 // a warp-wide look-back over per-tile descriptors, and written back with
 // coalesced stores.
 
-#include "gtc_internal.cuh"
+#include "scan_dev.cuh"
 
 namespace gtc {
 
@@ -20,58 +20,6 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_IPT;
 size_t scan_workspace_bytes(uint32_t n) {
   const uint32_t tiles = ceil_div(n > 0 ? n : 1, SCAN_TILE) + 1;
   return align_up((64 + (size_t)tiles) * 4, 256);
-}
-
-// Block-wide exclusive scan of one value per thread.  Returns the prefix and
-// the block total.
-template <int THREADS>
-__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
-  constexpr int WARPS = THREADS / 32;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const uint32_t incl = warp_inclusive_sum(v);
-  if (lane == 31) warp_sums[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    const uint32_t w = (lane < WARPS) ? warp_sums[lane] : 0u;
-    const uint32_t wi = warp_inclusive_sum(w);
-    if (lane < WARPS) warp_sums[lane] = wi - w;
-    if (lane == WARPS - 1) warp_sums[WARPS] = wi;
-  }
-  __syncthreads();
-  *total = warp_sums[WARPS];
-  return warp_sums[warp] + incl - v;
-}
-
-// Warp 0 chains this tile to its predecessors.  Publishes the aggregate,
-// looks back over a 32-tile window at a time and publishes the inclusive
-// prefix.  Returns the exclusive prefix of the tile (valid in lane 0..31).
-__device__ __forceinline__ uint32_t tile_lookback(uint32_t* desc, uint32_t tile, uint32_t aggregate,
-                                                  uint32_t* status) {
-  const int lane = threadIdx.x & 31;
-  if (tile == 0) {
-    if (lane == 0) st_relaxed(desc, (aggregate << 2) | FLAG_INCLUSIVE);
-    return 0;
-  }
-  if (lane == 0) st_relaxed(desc + tile, (aggregate << 2) | FLAG_AGGREGATE);
-  uint32_t excl = 0;
-  int k = (int)tile - 1 - lane;
-  while (true) {
-    const uint32_t v = (k >= 0) ? spin_descriptor(desc + k, status) : FLAG_INCLUSIVE;
-    const uint32_t incl_mask = __ballot_sync(0xffffffffu, (v & 3u) == FLAG_INCLUSIVE);
-    uint32_t contrib = v >> 2;
-    if (incl_mask) {
-      const int first = __ffs(incl_mask) - 1;  // closest inclusive predecessor
-      if (lane > first) contrib = 0;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
-    excl += contrib;
-    if (incl_mask) break;
-    k -= 32;
-  }
-  if (lane == 0) st_relaxed(desc + tile, ((excl + aggregate) << 2) | FLAG_INCLUSIVE);
-  return excl;
 }
 
 // ---------------------------------------------------------------- unique --
@@ -261,6 +209,12 @@ static cudaError_t launch_scan(const Launch& L, const uint32_t* in, uint32_t* ou
 cudaError_t launch_inclusive_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t n, void* ws) {
   if (n == 0) return cudaSuccess;
   return launch_scan(L, in, out, n, nullptr, n, 0, nullptr, ws);
+}
+
+cudaError_t launch_inclusive_scan_dev(const Launch& L, const uint32_t* in, uint32_t* out, const uint32_t* d_count,
+                                      uint32_t n_max, void* ws) {
+  if (n_max == 0) return cudaSuccess;
+  return launch_scan(L, in, out, 0, d_count, n_max, 0, nullptr, ws);
 }
 
 cudaError_t launch_node_offsets(const Launch& L, const uint32_t* edge, uint32_t* ps, const uint32_t* d_u,

@@ -307,6 +307,124 @@ class OctreePlan:
                             self.left[:m], self.parent[:m], self.edge[:m], self.ps[:u], self.nodes[:o], u, m, o)
 
 
+@dataclass
+class CloudResult:
+    """One cloud of a batched build: the same fields as OctreeResult, as
+    views into the batch's buffers (cloud-local indices)."""
+    keys: object
+    idx: object
+    prefix_n: object
+    has_leaf_left: object
+    has_leaf_right: object
+    left_child: object
+    parent: object
+    edge_count: object
+    node_offsets: object
+    nodes: object
+    n_unique: int
+    n_brt_nodes: int
+    n_oct_nodes: int
+
+
+class BatchPlan:
+    """Resident buffers for batched builds (gtc_build_octree_batched): up to
+    n_max points in up to clouds_max clouds, 32-bit codes.  offsets is a
+    device uint32 tensor of n_clouds + 1 non-decreasing point offsets."""
+
+    def __init__(self, ctx: Context, n_max: int, clouds_max: int, nodes_capacity: int | None = None):
+        torch = _torch()
+        self.ctx, self.n_max, self.clouds_max = ctx, n_max, clouds_max
+        dev = f"cuda:{ctx.device}"
+        n = max(n_max, 1)
+        i32, u8 = torch.int32, torch.uint8
+        self.keys = torch.empty(n, dtype=i32, device=dev)
+        self.idx = torch.empty(n, dtype=i32, device=dev)
+        self.prefix_n = torch.empty(n, dtype=u8, device=dev)
+        self.hll = torch.empty(n, dtype=u8, device=dev)
+        self.hlr = torch.empty(n, dtype=u8, device=dev)
+        self.left = torch.empty(n, dtype=i32, device=dev)
+        self.parent = torch.empty(n, dtype=i32, device=dev)
+        self.edge = torch.empty(n, dtype=i32, device=dev)
+        self.ps = torch.empty(n, dtype=i32, device=dev)
+        self.nodes_capacity = nodes_capacity or (n + clouds_max + 1024)
+        self.nodes = torch.empty((self.nodes_capacity, 16), dtype=i32, device=dev)
+        self.key_offset = torch.zeros(clouds_max + 1, dtype=i32, device=dev)
+        self.node_offset = torch.zeros(clouds_max + 1, dtype=i32, device=dev)
+        self.cloud_counts = torch.zeros((clouds_max, 3), dtype=i32, device=dev)
+        b = ctypes.c_size_t(0)
+        ctx.check(ctx.L.gtc_batched_workspace_size(n_max, clouds_max, ctypes.byref(b)))
+        self.ws = torch.empty(max(b.value, 256), dtype=torch.uint8, device=dev)
+        self.bufs = _lib.BatchBuffers(_ptr(self.keys), _ptr(self.idx), _ptr(self.prefix_n), _ptr(self.hll),
+                                      _ptr(self.hlr), _ptr(self.left), _ptr(self.parent), _ptr(self.edge),
+                                      _ptr(self.ps), _ptr(self.nodes), self.nodes_capacity, _ptr(self.key_offset),
+                                      _ptr(self.node_offset), _ptr(self.cloud_counts))
+        self.graph = None
+        self.n_clouds = 0
+
+    def launch(self, pts, offsets, n_total: int | None = None, min_coord=0.0, rng=1024.0, stream=None):
+        n_clouds = offsets.shape[0] - 1
+        n_total = pts.shape[0] if n_total is None else n_total
+        assert 1 <= n_clouds <= self.clouds_max and n_total <= self.n_max
+        self.n_clouds = n_clouds
+        self.ctx.check(self.ctx.L.gtc_build_octree_batched(
+            self.ctx.h, _ptr(pts), _ptr(offsets), n_clouds, n_total, min_coord, rng, ctypes.byref(self.bufs),
+            _ptr(self.ws), self.ws.numel(), _stream(stream)))
+
+    def capture(self, pts, offsets, n_total: int | None = None, min_coord=0.0, rng=1024.0):
+        """Capture the whole batched pipeline into one CUDA graph."""
+        torch = _torch()
+        self.launch(pts, offsets, n_total, min_coord, rng)  # warm-up (sets kernel attributes)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            g.capture_begin()
+            self.launch(pts, offsets, n_total, min_coord, rng, stream=s)
+            g.capture_end()
+        torch.cuda.synchronize()
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def host_offsets(self):
+        """(key_offset, node_offset, cloud_counts) as numpy arrays."""
+        S = self.n_clouds
+        return (self.key_offset[:S + 1].cpu().numpy().astype(np.int64),
+                self.node_offset[:S + 1].cpu().numpy().astype(np.int64),
+                self.cloud_counts[:S].cpu().numpy().astype(np.int64))
+
+    def clouds(self) -> list:
+        """Per-cloud results (raises on a device error, e.g. node capacity)."""
+        self.ctx.device_status()
+        ko, no, cc = self.host_offsets()
+        out = []
+        for c in range(self.n_clouds):
+            u, m, o = (int(x) for x in cc[c])
+            k0, n0 = int(ko[c]), int(no[c])
+            out.append(CloudResult(self.keys[k0:k0 + u], self.idx[k0:k0 + u], self.prefix_n[k0:k0 + m],
+                                   self.hll[k0:k0 + m], self.hlr[k0:k0 + m], self.left[k0:k0 + m],
+                                   self.parent[k0:k0 + m], self.edge[k0:k0 + m], self.ps[k0:k0 + u],
+                                   self.nodes[n0:n0 + o], u, m, o))
+        return out
+
+
+def build_octree_batched(ctx: Context, pts, offsets, min_coord=0.0, rng=1024.0) -> list:
+    """One batched build of the clouds pts[offsets[c]:offsets[c+1]] (device
+    tensors); returns per-cloud results, re-running once with a larger node
+    array if the first guess was too small."""
+    n_clouds = offsets.shape[0] - 1
+    plan = BatchPlan(ctx, pts.shape[0], n_clouds)
+    plan.launch(pts, offsets, min_coord=min_coord, rng=rng)
+    total_nodes = int(plan.node_offset[n_clouds].item())
+    if total_nodes > plan.nodes_capacity:
+        ctx.device_status_code()
+        plan = BatchPlan(ctx, pts.shape[0], n_clouds, nodes_capacity=total_nodes)
+        plan.launch(pts, offsets, min_coord=min_coord, rng=rng)
+    return plan.clouds()
+
+
 OP_LEARNED_SORT = 6
 LEARNED_FLAGS = {1: "overflow", 2: "order", 4: "non-monotone model", 8: "long run of equal keys"}
 

@@ -24,6 +24,14 @@ class OctreeBuffers(ctypes.Structure):
     ]
 
 
+class BatchBuffers(ctypes.Structure):
+    _fields_ = [
+        ("keys", P), ("idx", P), ("prefix_n", P), ("has_leaf_left", P), ("has_leaf_right", P),
+        ("left_child", P), ("parent", P), ("edge_count", P), ("node_offsets", P), ("nodes", P),
+        ("nodes_capacity", u32), ("key_offset", P), ("node_offset", P), ("cloud_counts", P),
+    ]
+
+
 SIGNATURES = {
     "gtc_create": (st, [ctypes.POINTER(P), i_]),
     "gtc_destroy": (st, [P]),
@@ -56,6 +64,8 @@ SIGNATURES = {
     "gtc_host_alloc": (st, [ctypes.POINTER(P), sz]),
     "gtc_host_free": (st, [P]),
     "gtc_sort_pairs_u32_noalloc": (st, [P, P, P, P, P, u32, i_, i_, P]),
+    "gtc_batched_workspace_size": (st, [u32, u32, ctypes.POINTER(sz)]),
+    "gtc_build_octree_batched": (st, [P, P, P, u32, u32, f32, f32, ctypes.POINTER(BatchBuffers), P, sz, P]),
     "gtc_learned_model_create": (st, [P, i_, ctypes.POINTER(P)]),
     "gtc_learned_model_destroy": (st, [P]),
     "gtc_learned_model_params": (st, [P, ctypes.POINTER(i_), ctypes.POINTER(P), ctypes.POINTER(P)]),

@@ -250,6 +250,47 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
                                          float range, int key_bits, gtc_octnode* host_nodes,
                                          uint32_t host_nodes_capacity, uint32_t* host_counts);
 
+/* ---------------------------------------------------- batched clouds ---- */
+/* No counterpart in the reference: many independent point clouds of uneven
+ * size built in one stream-ordered sequence of launches (graph-capturable, no
+ * host sync), 32-bit codes only.  Cloud c is points [off[c], off[c+1]) of
+ * pts; every cloud's outputs equal gtc_build_octree(key_bits = 32) on that
+ * cloud alone, with cloud-local indices:
+ *   keys, idx:                 [key_offset[c], key_offset[c] + u_c)
+ *   prefix_n .. edge_count:    [key_offset[c], key_offset[c] + m_c)
+ *   node_offsets:              [key_offset[c], key_offset[c] + u_c)
+ *   nodes:                     [node_offset[c], node_offset[c] + o_c)
+ * cloud_counts[3c .. 3c+2] = u_c, m_c, o_c; key_offset[n_clouds] = total
+ * unique codes; node_offset[n_clouds] = total nodes.  Every array is device
+ * memory; the per-code arrays hold n_total entries. */
+typedef struct gtc_batch_buffers {
+  uint32_t* keys;
+  uint32_t* idx;
+  uint8_t* prefix_n;
+  uint8_t* has_leaf_left;
+  uint8_t* has_leaf_right;
+  int32_t* left_child;
+  int32_t* parent;
+  uint32_t* edge_count;
+  uint32_t* node_offsets;
+  gtc_octnode* nodes;
+  uint32_t nodes_capacity;
+  uint32_t* key_offset;   /* [n_clouds + 1] */
+  uint32_t* node_offset;  /* [n_clouds + 1] */
+  uint32_t* cloud_counts; /* [3 * n_clouds] */
+} gtc_batch_buffers;
+
+/* Workspace of a batch (n_total < 2^30 points, 1 <= n_clouds <= 2^20). */
+GTC_API gtc_status gtc_batched_workspace_size(uint32_t n_total, uint32_t n_clouds, size_t* bytes);
+/* d_offsets: device uint32[n_clouds + 1], non-decreasing, d_offsets[0] = 0,
+ * d_offsets[n_clouds] = n_total; pts: device float[n_total][4]; ws: 256-byte
+ * aligned, gtc_batched_workspace_size bytes.  A node array that is too small
+ * sets GTC_ERR_CAPACITY in the device status word. */
+GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,
+                                            uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
+                                            const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
+                                            gtc_stream_t stream);
+
 /* The same sort of 32-bit keys (optionally with u32 values) for callers that
  * must not allocate device memory at the point where they sort: cudaMalloc /
  * cudaFree synchronise the device and can stall other streams for

@@ -65,3 +65,15 @@ def test_create_without_device_fails_cleanly(gtc_mod):
     h = ctypes.c_void_p()
     assert L.gtc_create(ctypes.byref(h), 0) == 3  # GTC_ERR_CUDA, no abort
     assert not h.value
+
+
+def test_batched_workspace_and_args_without_device(gtc_mod):
+    L = gtc_mod.lib()
+    b = ctypes.c_size_t()
+    assert L.gtc_batched_workspace_size(1_000_000, 512, ctypes.byref(b)) == 0
+    tiles = -(-1_000_000 // 6144) + 512  # per-cloud tiles never exceed n / tile + clouds
+    assert b.value >= 4 * tiles * 256 * 4 + 3 * 1_000_000 * 4 + 512 * 4 * 256 * 4
+    assert L.gtc_batched_workspace_size(1000, 0, ctypes.byref(b)) == 1  # no clouds
+    assert L.gtc_batched_workspace_size(1 << 30, 4, ctypes.byref(b)) == 1  # too many points
+    assert L.gtc_batched_workspace_size(1000, (1 << 20) + 1, ctypes.byref(b)) == 1  # too many clouds
+    assert L.gtc_build_octree_batched(None, None, None, 1, 0, 0.0, 1.0, None, None, 0, None) == 1

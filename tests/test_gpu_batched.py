@@ -1,0 +1,176 @@
+"""Parity of the batched build (gtc_build_octree_batched) with the oracle:
+every cloud of a batch must equal the oracle's single-cloud 32-bit build of
+that cloud alone, buffer for buffer and node for node (cloud-local indices)."""
+import numpy as np
+import pytest
+
+from gtc import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _p(xyz):
+    xyz = np.asarray(xyz, np.float32).reshape(-1, 3)
+    out = np.ones((xyz.shape[0], 4), np.float32)
+    out[:, :3] = xyz
+    return out
+
+
+def _batch(clouds):
+    sizes = [c.shape[0] for c in clouds]
+    offsets = np.zeros(len(clouds) + 1, np.uint32)
+    offsets[1:] = np.cumsum(sizes)
+    pts = np.concatenate(clouds) if sum(sizes) else np.zeros((0, 4), np.float32)
+    return np.ascontiguousarray(pts, np.float32), offsets
+
+
+def _check_cloud(gtc, oracle, res, pts_c, tag):
+    exp, _ = oracle.build_octree(pts_c, 32, threads=8)
+    assert exp["conflicts"] == 0
+    assert (res.n_unique, res.n_brt_nodes, res.n_oct_nodes) == (exp["n_unique"], exp["n_brt_nodes"],
+                                                                 exp["n_oct_nodes"]), tag
+    pairs = [("keys", res.keys, np.uint32), ("idx", res.idx, np.uint32), ("prefix_n", res.prefix_n, np.uint8),
+             ("has_leaf_left", res.has_leaf_left, np.uint8), ("has_leaf_right", res.has_leaf_right, np.uint8),
+             ("left_child", res.left_child, np.int32), ("parent", res.parent, np.int32),
+             ("edge_count", res.edge_count, np.uint32), ("node_offsets", res.node_offsets, np.uint32)]
+    for name, t, dt in pairs:
+        got = t.cpu().numpy().view(dt)
+        assert np.array_equal(got, exp[name]), (tag, name)
+    got_nodes = gtc.nodes_to_numpy(res.nodes)
+    assert np.array_equal(got_nodes.view(np.int32), exp["nodes"].view(np.int32)), (tag, "nodes")
+
+
+def _run_batch(ctx, oracle, pts, offsets, tag, check_every=1):
+    import gtc
+    import torch
+
+    tp = torch.from_numpy(pts).cuda() if pts.shape[0] else torch.zeros((0, 4), dtype=torch.float32, device="cuda")
+    to = torch.from_numpy(offsets.view(np.int32)).cuda()
+    results = gtc.build_octree_batched(ctx, tp, to)
+    assert len(results) == offsets.size - 1
+    for c in range(0, offsets.size - 1, check_every):
+        s, e = int(offsets[c]), int(offsets[c + 1])
+        _check_cloud(gtc, oracle, results[c], pts[s:e], f"{tag}/cloud{c}")
+    return results
+
+
+def test_batched_edge_cases(ctx, oracle):
+    clouds = [
+        np.zeros((0, 4), np.float32),                       # empty first cloud
+        _p([[1.0, 2.0, 3.0]]),                              # one point
+        _p([[1.0, 2.0, 3.0], [700.0, 2.0, 3.0]]),           # two points
+        _p([[5.5, 6.5, 7.5]] * 5000),                       # one distinct code
+        W.uniform_points(12_345, seed=3),                   # ragged last tile
+        np.zeros((0, 4), np.float32),                       # runs of empty clouds
+        np.zeros((0, 4), np.float32),
+        np.repeat(W.uniform_points(3000, seed=4), 7, axis=0),  # duplicates
+        W.gaussian_mixture_points(70_000, 1, 0.05, seed=6),  # dense cluster: long equal runs
+        _p([[1024.0, 0.0, 0.0], [0.0, 1023.99, 0.0], [0.0, 0.0, 0.0], [512.0, 512.0, 512.0]]),
+        _p([[float(i) * 0.25, 1.0, 1.0] for i in range(4096)]),
+        W.uniform_points(6144, seed=9),                     # exactly one sort tile
+        W.uniform_points(6145, seed=10),                    # one tile + one key
+        _p([[9.0, 9.0, 9.0]]),                              # one point, last cloud
+        np.zeros((0, 4), np.float32),                       # empty last cloud
+    ]
+    pts, offsets = _batch(clouds)
+    _run_batch(ctx, oracle, pts, offsets, "edge")
+
+
+def test_batched_config4_reduced(ctx, oracle):
+    """64 clouds, sizes log-uniform in [1K, 100K], alternately uniform and
+    8-cluster Gaussian (the batched workload's shape at reduced size)."""
+    pts, offsets = W.config4_clouds(64, seed=1, lo=1000, hi=100_000)
+    _run_batch(ctx, oracle, pts, offsets, "config4-reduced")
+
+
+def test_batched_config4_full(ctx, oracle):
+    """The full batched workload: 512 clouds, sizes log-uniform in [1K, 1M];
+    every eighth cloud is checked against the oracle in full, and every cloud
+    by size-independent properties (sorted unique codes, a valid octree)."""
+    import gtc
+
+    pts, offsets = W.config4_clouds(512, seed=0)
+    results = _run_batch(ctx, oracle, pts, offsets, "config4", check_every=8)
+    for c, res in enumerate(results):
+        keys = res.keys.cpu().numpy().view(np.uint32).astype(np.int64)
+        assert res.n_unique >= 1 and np.all(np.diff(keys) > 0), c
+        assert oracle.validate_octree(gtc.nodes_to_numpy(res.nodes), res.n_unique) == 0, c
+
+
+def test_batched_graph_replay(ctx, oracle):
+    import gtc
+    import torch
+
+    pts, offsets = W.config4_clouds(24, seed=5, lo=100, hi=50_000)
+    tp = torch.from_numpy(pts).cuda()
+    to = torch.from_numpy(offsets.view(np.int32)).cuda()
+    plan = gtc.BatchPlan(ctx, pts.shape[0], offsets.size - 1)
+    plan.capture(tp, to)
+    for _ in range(3):
+        plan.replay()
+    torch.cuda.synchronize()
+    for c, res in enumerate(plan.clouds()):
+        s, e = int(offsets[c]), int(offsets[c + 1])
+        _check_cloud(gtc, oracle, res, pts[s:e], f"graph/cloud{c}")
+
+
+def test_batched_all_empty(ctx):
+    import gtc
+    import torch
+
+    plan = gtc.BatchPlan(ctx, 16, 3)
+    offsets = torch.zeros(4, dtype=torch.int32, device="cuda")
+    plan.launch(torch.zeros((0, 4), dtype=torch.float32, device="cuda"), offsets, n_total=0)
+    ko, no, cc = plan.host_offsets()
+    assert not ko.any() and not no.any() and not cc.any()
+    assert [r.n_unique for r in plan.clouds()] == [0, 0, 0]
+
+
+def test_batched_node_capacity_reported(ctx):
+    """A node array that is too small is reported as a capacity error; the
+    kernels store nothing past it."""
+    import gtc
+    import torch
+
+    pts, offsets = _batch([W.uniform_points(5000, seed=1), W.uniform_points(7000, seed=2)])
+    tp = torch.from_numpy(pts).cuda()
+    to = torch.from_numpy(offsets.view(np.int32)).cuda()
+    plan = gtc.BatchPlan(ctx, pts.shape[0], 2, nodes_capacity=100)
+    plan.launch(tp, to)
+    with pytest.raises(gtc.GtcError) as ei:
+        plan.ctx.device_status()
+    assert ei.value.status == 7
+    big = gtc.BatchPlan(ctx, pts.shape[0], 2)
+    big.launch(tp, to)
+    assert int(big.node_offset[2].item()) > 100
+    big.clouds()
+
+
+@pytest.mark.parametrize("offs", [[0, 100, 50, 200], [0, 100, 150, 199], [5, 100, 150, 200]])
+def test_batched_bad_device_offsets(ctx, offs):
+    """Offsets that do not partition [0, n_total) are caught on the device:
+    the status reads INVALID_ARG and the batch reports no codes, no nodes."""
+    import gtc
+    import torch
+
+    pts = torch.from_numpy(W.uniform_points(200, seed=1)).cuda()
+    plan = gtc.BatchPlan(ctx, 200, 3)
+    plan.launch(pts, torch.tensor(offs, dtype=torch.int32, device="cuda"), n_total=200)
+    with pytest.raises(gtc.GtcError) as ei:
+        ctx.device_status()
+    assert ei.value.status == 1
+    ko, no, cc = plan.host_offsets()
+    assert not ko.any() and not no.any() and not cc.any()
+
+
+def test_batched_rejects_bad_args(ctx):
+    import gtc
+    import torch
+
+    plan = gtc.BatchPlan(ctx, 64, 2)
+    pts = torch.zeros((64, 4), dtype=torch.float32, device="cuda")
+    offsets = torch.tensor([0, 32, 64], dtype=torch.int32, device="cuda")
+    # Points not 16-byte aligned: refused on the host before any launch.
+    with pytest.raises(gtc.GtcError) as ei:
+        plan.launch(pts.view(-1)[1:], offsets, n_total=64)
+    assert ei.value.status == 1
