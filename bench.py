@@ -211,6 +211,12 @@ def run_gtc(args):
     pts_np = W.config2_points(n, seed=rank)
     pts = torch.from_numpy(pts_np).to(dev)
     ctx = gtc.Context(local)
+    # Autotune the onesweep shape on this workload's own Morton codes (the
+    # pipeline's sort: 63 bits of 64-bit keys); the choice is cached per
+    # (key width, bits, ceil(log2 n)) and picked up by the build below.
+    codes, _ = ctx.morton(pts, KEY_BITS, with_idx=False)
+    tune = ctx.autotune_sort(KEY_BITS, n, 0, 63, keys=codes, reps=3)
+    del codes
     plan = gtc.OctreePlan(ctx, n, KEY_BITS, nodes_capacity=n + (n >> 1))
     for _ in range(max(args.warmup, 3)):
         plan.launch(pts)
@@ -315,7 +321,8 @@ def run_gtc(args):
                    "graph_ms_per_step": round(graph_ms, 4), "stage_ms_per_step": stage_ms,
                    "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
                    "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
-                   "sort_variant": ctx.get_sort_variant(64)},
+                   "sort_variant": gtc.autotune_lookup(KEY_BITS, 63, n),
+                   "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,

@@ -275,12 +275,17 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
                                const SortWorkspace& W, int passes);
-template <class K>
-int sort_tile_keys(uint32_t n);
+// variant < 0: the pinned variant, else the autotuned one for (key width,
+// bits, n), else the built-in default.
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
-                                   bool* result_in_alt, cudaEvent_t* ev_pass /* nullable [2*passes] */);
+                                   bool* result_in_alt, cudaEvent_t* ev_pass /* nullable [2*passes] */,
+                                   int variant = -1);
+// The variant a sort of n keys of key_bits width over `bits` bits will use.
+int sort_select_variant(int key_bits, int bits, uint32_t n);
+// Autotuner cache (tune.cu): the tuned variant for (key width, bits, n), or -1.
+int tuned_variant(int key_bits, int bits, uint32_t n);
 
 // Decoupled look-back scans: unique compaction and node offsets.
 size_t scan_workspace_bytes(uint32_t n);

@@ -498,7 +498,15 @@ struct Variant {
 constexpr Variant kVariants[] = {{256, 16, 0}, {384, 16, 0}, {512, 12, 0},
                                  {256, 16, 1}, {256, 16, 2}, {512, 8, 2}, {256, 24, 2}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 before autotuning
+static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
+static int g_pinned[2] = {-1, -1};  // gtc_sort_set_variant: overrides the tuned choice
+
+int sort_select_variant(int key_bits, int bits, uint32_t n) {
+  const int w = key_bits == 64;
+  if (g_pinned[w] >= 0) return g_pinned[w];
+  const int t = tuned_variant(key_bits, bits, n);
+  return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
+}
 
 template <class K, int THREADS, int KPT, bool HV>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
@@ -567,14 +575,6 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
 #undef GTC_TMA
 }
 
-template <class K>
-int sort_tile_keys(uint32_t) {
-  const Variant& v = kVariants[g_variant[sizeof(K) == 8]];
-  return v.threads * v.kpt;
-}
-template int sort_tile_keys<uint32_t>(uint32_t);
-template int sort_tile_keys<uint64_t>(uint32_t);
-
 // Smallest tile of any variant: sizes the descriptor array for every variant.
 static int min_tile_keys() {
   int t = 1 << 30;
@@ -637,8 +637,9 @@ template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, 
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
-                                   bool* result_in_alt, cudaEvent_t* ev) {
-  const int v = g_variant[sizeof(K) == 8];
+                                   bool* result_in_alt, cudaEvent_t* ev, int variant) {
+  const int v = (variant >= 0 && variant < kNumVariants) ? variant
+                                                          : sort_select_variant(8 * sizeof(K), end_bit - begin_bit, n);
   const bool hv = vals != nullptr;
   K* src_k = keys;
   K* dst_k = keys_alt;
@@ -665,16 +666,20 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
 }
 template cudaError_t launch_onesweep_passes<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*);
+                                                      cudaEvent_t*, int);
 template cudaError_t launch_onesweep_passes<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*);
+                                                      cudaEvent_t*, int);
 
 int sort_num_variants() { return kNumVariants; }
-int sort_get_variant(int key_bits) { return g_variant[key_bits == 64]; }
+int sort_get_variant(int key_bits) {
+  const int w = key_bits == 64;
+  return g_pinned[w] >= 0 ? g_pinned[w] : g_variant[w];
+}
+// v = -1 unpins (back to tuned / default selection).
 bool sort_set_variant(int key_bits, int v) {
-  if (v < 0 || v >= kNumVariants) return false;
-  g_variant[key_bits == 64] = v;
+  if (v < -1 || v >= kNumVariants) return false;
+  g_pinned[key_bits == 64] = v;
   return true;
 }
 void sort_variant_shape(int v, int* threads, int* kpt) {

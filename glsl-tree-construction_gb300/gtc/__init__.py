@@ -224,6 +224,38 @@ class Context:
     def get_sort_variant(self, key_bits: int) -> int:
         return int(self.L.gtc_sort_get_variant(key_bits))
 
+    def autotune_sort(self, key_bits: int, n: int, begin_bit: int = 0, end_bit: int | None = None, keys=None,
+                      reps: int = 3) -> dict:
+        """Time every onesweep variant on n keys (the given device keys, or
+        seeded uniform ones) and cache the fastest for this shape.  Returns
+        {"best": variant, "ms": [per-variant best time]}."""
+        end_bit = key_bits if end_bit is None else end_bit
+        nv = self.L.gtc_sort_num_variants()
+        times = (ctypes.c_float * nv)()
+        best = ctypes.c_int(-1)
+        self.check(self.L.gtc_autotune_sort(self.h, key_bits, begin_bit, end_bit, n, _ptr(keys), reps,
+                                            ctypes.byref(best), times))
+        return {"best": best.value, "ms": [float(t) for t in times]}
+
+
+def autotune_lookup(key_bits: int, bits: int, n: int) -> int:
+    """The autotuned onesweep variant for a sort of that shape, or -1."""
+    return int(lib().gtc_autotune_lookup(key_bits, bits, n))
+
+
+def autotune_save(path: str):
+    if lib().gtc_autotune_save(path.encode()) != 0:
+        raise GtcError(1, f"cannot write {path}")
+
+
+def autotune_load(path: str):
+    if lib().gtc_autotune_load(path.encode()) != 0:
+        raise GtcError(1, f"cannot read {path}")
+
+
+def autotune_clear():
+    lib().gtc_autotune_clear()
+
 
 @dataclass
 class OctreeResult:

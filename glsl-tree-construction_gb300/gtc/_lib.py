@@ -78,6 +78,13 @@ SIGNATURES = {
     "gtc_sort_variant_shape": (st, [i_, ctypes.POINTER(i_), ctypes.POINTER(i_)]),
     "gtc_sort_set_variant": (st, [i_, i_]),
     "gtc_sort_get_variant": (i_, [i_]),
+    "gtc_autotune_sort": (st, [P, i_, i_, i_, u32, P, i_, ctypes.POINTER(i_), P]),
+    "gtc_autotune_lookup": (i_, [i_, i_, u32]),
+    "gtc_autotune_record": (st, [i_, i_, u32, i_, f32]),
+    "gtc_autotune_clear": (st, []),
+    "gtc_autotune_entries": (i_, []),
+    "gtc_autotune_save": (st, [ctypes.c_char_p]),
+    "gtc_autotune_load": (st, [ctypes.c_char_p]),
     # reference-signature host shims
     "gtc_ref_compute_morton": (st, [P, P, u32, f32, f32, u32]),
     "gtc_ref_morton32_to_xyz": (None, [P, u32, f32, f32]),

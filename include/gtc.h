@@ -361,8 +361,28 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
  * reference counterpart: the reference hard-codes 512 x 15 (main.rs:182). */
 GTC_API int gtc_sort_num_variants(void);
 GTC_API gtc_status gtc_sort_variant_shape(int variant, int* threads, int* keys_per_thread);
+/* Pins one variant for every sort of that key width (overriding the tuned
+ * choice); variant = -1 unpins. */
 GTC_API gtc_status gtc_sort_set_variant(int key_bits, int variant);
 GTC_API int gtc_sort_get_variant(int key_bits);
+
+/* Autotuner.  Times every variant on n keys of key_bits width sorted over
+ * [begin_bit, end_bit) - the caller's device keys d_sample_keys (n of them,
+ * nullable) or seeded uniform keys - taking the best of `reps` timed runs
+ * after one warm-up, and caches the fastest for (key_bits, end_bit -
+ * begin_bit, ceil(log2 n)).  best_variant and times_ms[gtc_sort_num_variants()]
+ * are nullable.  Synchronous; allocates its own buffers.  The cache is
+ * process-wide; the file named by the environment variable GTC_TUNE_CACHE is
+ * loaded on first use and rewritten after each tuning. */
+GTC_API gtc_status gtc_autotune_sort(gtc_ctx* ctx, int key_bits, int begin_bit, int end_bit, uint32_t n,
+                                     const void* d_sample_keys, int reps, int* best_variant, float* times_ms);
+/* The cached variant for a sort of that shape, or -1. */
+GTC_API int gtc_autotune_lookup(int key_bits, int bits, uint32_t n);
+GTC_API gtc_status gtc_autotune_record(int key_bits, int bits, uint32_t n, int variant, float ms);
+GTC_API gtc_status gtc_autotune_clear(void);
+GTC_API int gtc_autotune_entries(void);
+GTC_API gtc_status gtc_autotune_save(const char* path);
+GTC_API gtc_status gtc_autotune_load(const char* path);
 
 /* Pinned host memory helpers for callers without a CUDA runtime binding. */
 GTC_API gtc_status gtc_host_alloc(void** ptr, size_t bytes);

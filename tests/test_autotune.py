@@ -1,0 +1,71 @@
+"""The onesweep autotuner's cache (tune.cu): record / lookup per (key width,
+bits, ceil(log2 n)), text persistence, and the GTC_TUNE_CACHE file loaded on
+first use.  Host logic only; the timing itself is in test_gpu_autotune.py."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture()
+def clean(gtc_mod):
+    gtc_mod.autotune_clear()
+    yield gtc_mod
+    gtc_mod.autotune_clear()
+
+
+def test_record_and_lookup_by_size_bucket(clean):
+    g = clean
+    L = g.lib()
+    assert g.autotune_lookup(64, 63, 10_000_000) == -1
+    assert L.gtc_autotune_record(64, 63, 10_000_000, 2, 0.61) == 0
+    # ceil(log2 n) buckets: 2^23 < n <= 2^24 share the entry
+    assert g.autotune_lookup(64, 63, (1 << 23) + 1) == 2
+    assert g.autotune_lookup(64, 63, 1 << 24) == 2
+    assert g.autotune_lookup(64, 63, 1 << 23) == -1
+    assert g.autotune_lookup(64, 64, 10_000_000) == -1  # another bit count
+    assert g.autotune_lookup(32, 63, 10_000_000) == -1  # another key width
+    assert L.gtc_autotune_entries() == 1
+
+
+def test_record_rejects_bad_entries(clean):
+    L = clean.lib()
+    nv = L.gtc_sort_num_variants()
+    assert L.gtc_autotune_record(48, 30, 100, 0, 1.0) == 1
+    assert L.gtc_autotune_record(32, 33, 100, 0, 1.0) == 1
+    assert L.gtc_autotune_record(32, 30, 100, nv, 1.0) == 1
+    assert L.gtc_autotune_record(32, 30, 100, -1, 1.0) == 1
+    assert L.gtc_autotune_entries() == 0
+
+
+def test_save_load_roundtrip_and_malformed_lines(clean, tmp_path):
+    g = clean
+    L = g.lib()
+    assert L.gtc_autotune_record(32, 30, 1 << 20, 1, 0.2) == 0
+    assert L.gtc_autotune_record(64, 63, 10_000_000, 2, 0.6) == 0
+    path = str(tmp_path / "tune.txt")
+    g.autotune_save(path)
+    g.autotune_clear()
+    assert L.gtc_autotune_entries() == 0
+    with open(path, "a") as f:
+        f.write("garbage line\nsort 64 63 25 999 1.0\nsort 16 8 3 0 1.0\n")  # ignored
+    g.autotune_load(path)
+    assert L.gtc_autotune_entries() == 2
+    assert g.autotune_lookup(32, 30, 1 << 20) == 1
+    assert g.autotune_lookup(64, 63, 10_000_000) == 2
+    with pytest.raises(g.GtcError):
+        g.autotune_load(str(tmp_path / "missing.txt"))
+
+
+def test_env_cache_file_is_loaded_on_first_use(tmp_path):
+    path = tmp_path / "env_tune.txt"
+    path.write_text("sort 64 63 24 3 0.5\n")
+    code = ("import sys; sys.path.insert(0, %r); import gtc; "
+            "print(gtc.autotune_lookup(64, 63, 10_000_000))" % os.path.join(REPO, "glsl-tree-construction_gb300"))
+    env = dict(os.environ, GTC_TUNE_CACHE=str(path))
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == "3"
