@@ -33,6 +33,7 @@ for _p in (REPO, os.path.join(REPO, "glsl-tree-construction_gb300")):
 METRIC = "Mpoints/s full octree build"
 UNIT = "Mpoints/s"
 N_POINTS = 10_000_000
+LEARNED_KEYS = 64 << 20
 KEY_BITS = 64
 WORKLOAD = "octree_clustered_10M_u64"
 FALLBACK_HBM_GBS = 6800.0
@@ -44,7 +45,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["gtc", "reference"], default="gtc")
-    ap.add_argument("--n", type=int, default=N_POINTS, help="points (default: the 10M workload)")
+    ap.add_argument("--n", type=int, default=None,
+                    help="points / keys (default: 10M for octree and sort, 64M (2^26) for learned)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["octree", "sort", "learned", "batched"], default="octree",
                     help="octree: the 10M clustered full build (default); sort: onesweep pairs sort only; "
@@ -661,6 +663,8 @@ def run_gtc_batched(args):
 
 def main():
     args = parse_args()
+    if args.n is None:
+        args.n = LEARNED_KEYS if args.workload == "learned" else N_POINTS
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "sort":

@@ -317,9 +317,12 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
       GTC_TRY(ctx, launch_unique<K>(L, keys_alt, vals_alt, keys, o->idx, n, o->counts + 0, scan_ws));
   }
   {
+    // vals_alt is free once unique has compacted: it holds the queue of
+    // long-range splits; a spare word of the scan workspace counts them.
     StageTimer t(ctx, stream, GTC_STAGE_RADIX_TREE);
     GTC_TRY(ctx, launch_radix_tree<K>(L, keys, o->counts + 0, 0, n, o->prefix_n, o->has_leaf_left, o->has_leaf_right,
-                                      o->left_child, o->parent, o->edge_count, o->counts + 1));
+                                      o->left_child, o->parent, o->edge_count, o->counts + 1, vals_alt,
+                                      reinterpret_cast<uint32_t*>(scan_ws) + 32));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_PREFIX_SUM);
@@ -719,5 +722,7 @@ GTC_API gtc_status gtc_sort_set_variant(int key_bits, int v) {
   return sort_set_variant(key_bits, v) ? GTC_OK : GTC_ERR_INVALID_ARG;
 }
 GTC_API int gtc_sort_get_variant(int key_bits) { return sort_get_variant(key_bits); }
+GTC_API gtc_status gtc_tree_set_method(int method) { return tree_set_method(method) ? GTC_OK : GTC_ERR_INVALID_ARG; }
+GTC_API int gtc_tree_get_method(void) { return tree_get_method(); }
 
 }  // extern "C"

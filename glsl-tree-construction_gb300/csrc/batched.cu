@@ -29,6 +29,7 @@
 #include "karras.cuh"
 #include "octree_dev.cuh"
 #include "scan_dev.cuh"
+#include "tree_window.cuh"
 
 namespace gtc {
 
@@ -59,23 +60,6 @@ constexpr int BU_THREADS = 512;
 constexpr int BU_IPT = 9;
 constexpr int BU_TILE = BU_THREADS * BU_IPT;  // the scan tile of scan.cu
 constexpr uint32_t MAX_CLOUDS = 1u << 20;
-
-// First index in a[0..n) with a[i] > x.
-__device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t n, uint32_t x) {
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (a[mid] <= x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// The cloud that owns position x of a run of offsets off[0..S] (off[S] > x):
-// the last c with off[c] <= x, which skips empty clouds.
-__device__ __forceinline__ uint32_t owner(const uint32_t* off, uint32_t S, uint32_t x) {
-  return upper_bound_u32(off, S + 1, x) - 1;
-}
 
 // Tiles per cloud and non-empty clouds, both scanned (one block).  The
 // offsets must partition [0, n): off[0] = 0, non-decreasing, off[S] = n.
@@ -611,9 +595,21 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   }
   {
     Stage t(ctx, stream, GTC_STAGE_RADIX_TREE);
-    const uint32_t grid = max(1u, min(ceil_div(n_total, 256), (uint32_t)L.num_sms * 8));
-    bt_tree_kernel<<<grid, 256, 0, s>>>(out->keys, out->key_offset, S, out->prefix_n, out->has_leaf_left,
-                                        out->has_leaf_right, out->left_child, out->parent, out->edge_count);
+    if (tree_get_method() == 1) {
+      // idx_alt is free after unique: the queue of long-range splits.
+      uint32_t* q_count = W.counters + 16;  // zeroed with the counters
+      radix_tree_window_kernel<uint32_t, true><<<ceil_div(n_total, TW_T), TW_THREADS, 0, s>>>(
+          out->keys, nullptr, 0, out->key_offset, S, out->prefix_n, out->has_leaf_left, out->has_leaf_right,
+          out->left_child, out->parent, out->edge_count, nullptr, W.idx_alt, q_count);
+      BCHK(cudaGetLastError());
+      radix_tree_slow_kernel<uint32_t, true><<<L.num_sms * 2, 256, 0, s>>>(
+          out->keys, nullptr, 0, out->key_offset, S, out->prefix_n, out->has_leaf_left, out->has_leaf_right,
+          out->left_child, out->parent, out->edge_count, W.idx_alt, q_count);
+    } else {
+      const uint32_t grid = max(1u, min(ceil_div(n_total, 256), (uint32_t)L.num_sms * 8));
+      bt_tree_kernel<<<grid, 256, 0, s>>>(out->keys, out->key_offset, S, out->prefix_n, out->has_leaf_left,
+                                          out->has_leaf_right, out->left_child, out->parent, out->edge_count);
+    }
     BCHK(cudaGetLastError());
   }
   {

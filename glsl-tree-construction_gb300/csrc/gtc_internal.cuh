@@ -304,7 +304,12 @@ cudaError_t launch_node_offsets(const Launch& L, const uint32_t* edge, uint32_t*
 template <class K>
 cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d_u, int32_t m_host, uint32_t n_max,
                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int32_t* left, int32_t* parent,
-                              uint32_t* edge, uint32_t* d_m /* nullable: receives m */);
+                              uint32_t* edge, uint32_t* d_m /* nullable: receives m */,
+                              uint32_t* queue = nullptr /* n_max words: long-range splits go to a warp pass */,
+                              uint32_t* q_count = nullptr /* one word, zeroed here */);
+// Radix tree method: 1 split-indexed window kernel (default), 0 per-node Karras.
+int tree_get_method();
+bool tree_set_method(int m);
 cudaError_t launch_edge_count(const Launch& L, const uint8_t* prefix_n, const int32_t* parent, uint32_t* edge,
                               uint32_t m, int unused_bits);
 template <class K>

@@ -10,10 +10,20 @@
 // searches that make up most nodes.
 
 #include "karras.cuh"
+#include "tree_window.cuh"
 
 namespace gtc {
 
 constexpr int TREE_THREADS = 256;
+
+// 1: split-indexed window kernel (tree_window.cuh); 0: per-node Karras search.
+static int g_tree_method = 1;
+int tree_get_method() { return g_tree_method; }
+bool tree_set_method(int m) {
+  if (m != 0 && m != 1) return false;
+  g_tree_method = m;
+  return true;
+}
 
 template <class K>
 __global__ void __launch_bounds__(TREE_THREADS) radix_tree_kernel(const K* __restrict__ codes, const uint32_t* d_u,
@@ -39,18 +49,33 @@ __global__ void __launch_bounds__(TREE_THREADS) radix_tree_kernel(const K* __res
 template <class K>
 cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d_u, int32_t m_host, uint32_t n_max,
                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int32_t* left, int32_t* parent,
-                              uint32_t* edge, uint32_t* d_m) {
+                              uint32_t* edge, uint32_t* d_m, uint32_t* queue, uint32_t* q_count) {
   const uint32_t work = d_u ? n_max : (uint32_t)max(m_host, 0);
   if (work == 0 && !d_m) return cudaSuccess;
+  if (g_tree_method == 1) {
+    const uint32_t u_host = d_u ? 0u : (uint32_t)max(m_host, 0) + 1;
+    if (queue) {
+      cudaError_t e = cudaMemsetAsync(q_count, 0, 4, L.stream);
+      if (e != cudaSuccess) return e;
+    }
+    radix_tree_window_kernel<K, false><<<max(1u, ceil_div(work, TW_T)), TW_THREADS, 0, L.stream>>>(
+        codes, d_u, u_host, nullptr, 0, prefix_n, hll, hlr, left, parent, edge, d_m, queue, q_count);
+    if (queue)
+      radix_tree_slow_kernel<K, false><<<L.num_sms * 2, 256, 0, L.stream>>>(
+          codes, d_u, u_host, nullptr, 0, prefix_n, hll, hlr, left, parent, edge, queue, q_count);
+    return cudaGetLastError();
+  }
   const uint32_t grid = max(1u, min(ceil_div(work, TREE_THREADS), (uint32_t)L.num_sms * 8));
   radix_tree_kernel<K><<<grid, TREE_THREADS, 0, L.stream>>>(codes, d_u, m_host, prefix_n, hll, hlr, left, parent,
                                                              edge, d_m);
   return cudaGetLastError();
 }
 template cudaError_t launch_radix_tree<uint32_t>(const Launch&, const uint32_t*, const uint32_t*, int32_t, uint32_t,
-                                                 uint8_t*, uint8_t*, uint8_t*, int32_t*, int32_t*, uint32_t*, uint32_t*);
+                                                 uint8_t*, uint8_t*, uint8_t*, int32_t*, int32_t*, uint32_t*, uint32_t*,
+                                                 uint32_t*, uint32_t*);
 template cudaError_t launch_radix_tree<uint64_t>(const Launch&, const uint64_t*, const uint32_t*, int32_t, uint32_t,
-                                                 uint8_t*, uint8_t*, uint8_t*, int32_t*, int32_t*, uint32_t*, uint32_t*);
+                                                 uint8_t*, uint8_t*, uint8_t*, int32_t*, int32_t*, uint32_t*, uint32_t*,
+                                                 uint32_t*, uint32_t*);
 
 // edge_count.comp:30-41 over exactly m nodes, depth = (prefix_n - A) / 3.
 __global__ void edge_count_kernel(const uint8_t* __restrict__ prefix_n, const int32_t* __restrict__ parent,

@@ -78,6 +78,8 @@ SIGNATURES = {
     "gtc_sort_variant_shape": (st, [i_, ctypes.POINTER(i_), ctypes.POINTER(i_)]),
     "gtc_sort_set_variant": (st, [i_, i_]),
     "gtc_sort_get_variant": (i_, [i_]),
+    "gtc_tree_set_method": (st, [i_]),
+    "gtc_tree_get_method": (i_, []),
     "gtc_autotune_sort": (st, [P, i_, i_, i_, u32, P, i_, ctypes.POINTER(i_), P]),
     "gtc_autotune_lookup": (i_, [i_, i_, u32]),
     "gtc_autotune_record": (st, [i_, i_, u32, i_, f32]),

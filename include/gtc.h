@@ -366,6 +366,13 @@ GTC_API gtc_status gtc_sort_variant_shape(int variant, int* threads, int* keys_p
 GTC_API gtc_status gtc_sort_set_variant(int key_bits, int variant);
 GTC_API int gtc_sort_get_variant(int key_bits);
 
+/* Radix tree method, process-wide: 1 (default) builds each node from its
+ * split with nearest-smaller queries over a shared-memory window of
+ * adjacent-key prefix lengths; 0 runs the per-node Karras searches of
+ * build_radix_tree.comp:71-144.  Both give identical output. */
+GTC_API gtc_status gtc_tree_set_method(int method);
+GTC_API int gtc_tree_get_method(void);
+
 /* Autotuner.  Times every variant on n keys of key_bits width sorted over
  * [begin_bit, end_bit) - the caller's device keys d_sample_keys (n of them,
  * nullable) or seeded uniform keys - taking the best of `reps` timed runs

@@ -76,11 +76,18 @@ def test_batched_edge_cases(ctx, oracle):
     _run_batch(ctx, oracle, pts, offsets, "edge")
 
 
-def test_batched_config4_reduced(ctx, oracle):
+@pytest.mark.parametrize("tree_method", [1, 0], ids=["window", "karras"])
+def test_batched_config4_reduced(ctx, oracle, gtc_mod, tree_method):
     """64 clouds, sizes log-uniform in [1K, 100K], alternately uniform and
-    8-cluster Gaussian (the batched workload's shape at reduced size)."""
-    pts, offsets = W.config4_clouds(64, seed=1, lo=1000, hi=100_000)
-    _run_batch(ctx, oracle, pts, offsets, "config4-reduced")
+    8-cluster Gaussian (the batched workload's shape at reduced size), with
+    both radix tree kernels."""
+    L = gtc_mod.lib()
+    assert L.gtc_tree_set_method(tree_method) == 0
+    try:
+        pts, offsets = W.config4_clouds(64, seed=1, lo=1000, hi=100_000)
+        _run_batch(ctx, oracle, pts, offsets, "config4-reduced")
+    finally:
+        L.gtc_tree_set_method(1)
 
 
 def test_batched_config4_full(ctx, oracle):

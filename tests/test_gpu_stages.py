@@ -161,9 +161,22 @@ def _unique_codes(oracle, pts, key_bits):
     return ku
 
 
+@pytest.fixture(params=[1, 0], ids=["window", "karras"])
+def tree_method(request, gtc_mod):
+    """Both radix tree kernels: the split-indexed window kernel and the
+    per-node Karras search."""
+    L = gtc_mod.lib()
+    assert L.gtc_tree_set_method(request.param) == 0
+    yield request.param
+    L.gtc_tree_set_method(1)
+
+
 @pytest.mark.parametrize("key_bits", [32, 64])
-def test_radix_tree_and_edge_count(ctx, oracle, key_bits):
-    for name, pts in pts_cases().items():
+def test_radix_tree_and_edge_count(ctx, oracle, key_bits, tree_method):
+    cases = dict(pts_cases())
+    # long ranges: most top-level splits reach past a block's halo
+    cases["spread_clusters"] = W.gaussian_mixture_points(400_000, 3, 0.02, noise=0.001, seed=17)
+    for name, pts in cases.items():
         codes = _unique_codes(oracle, pts, key_bits)
         m = codes.size - 1
         t = ctx.radix_tree(dev(codes), m, with_edge=True)
