@@ -17,8 +17,10 @@
 //               publishes an inclusive prefix at once);
 //   4. unique:  compaction that restarts at every cloud start; cloud c's
 //               unique codes land at [U_c, U_{c+1});
-//   5. radix tree of each cloud (karras_node on the cloud's codes) with the
-//               edge counts, and a zero edge in each cloud's last slot;
+//   5. radix tree of each cloud (the window kernel of tree_window.cuh, with
+//               pairs that straddle two clouds as boundaries; karras_node
+//               under the per-node method) with the edge counts, and a zero
+//               edge in each cloud's last slot;
 //   6. one inclusive scan of all edge counts; cloud c's node offsets are the
 //               scan minus its value just before U_c (the bias);
 //   7. octree of each cloud (octree_make_node) into its node range starting
@@ -402,9 +404,11 @@ __global__ void __launch_bounds__(256) bt_tree_kernel(const uint32_t* __restrict
   }
 }
 
-// Per cloud: u, m, o and the first node slot O_c, from the global scan.
+// Per cloud: u, m, o and the first node slot O_c, from the global scan; and
+// the cloud's (U0, U1, bias, O_c) for the octree kernel.
 __global__ void bt_cloud_offsets_kernel(uint32_t* uoff, const uint32_t* ne_start, const uint32_t* ps, uint32_t S,
-                                        uint32_t* node_off, uint32_t* cloud_counts, const uint32_t* bad) {
+                                        uint32_t* node_off, uint32_t* cloud_counts, uint4* cinfo,
+                                        const uint32_t* bad) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S) return;
   if (*bad) {
@@ -420,44 +424,80 @@ __global__ void bt_cloud_offsets_kernel(uint32_t* uoff, const uint32_t* ne_start
   const uint32_t O = ne_start[c] + bias;
   const uint32_t o = u > 0 ? 1 + ps[U1 - 1] - bias : 0u;
   node_off[c] = O;
+  cinfo[c] = make_uint4(U0, U1, bias, O);
   cloud_counts[3 * c + 0] = u;
   cloud_counts[3 * c + 1] = u > 0 ? u - 1 : 0u;
   cloud_counts[3 * c + 2] = o;
   if (c == S - 1) node_off[S] = O + o;
 }
 
-// Octree of every cloud, one thread per unique code; also the cloud-local
-// node offsets (what the single-cloud node-offset scan gives each cloud).
-__global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restrict__ codes, const uint32_t* uoff,
-                                                        uint32_t S, const uint8_t* prefix_n, const uint8_t* hll,
-                                                        const uint8_t* hlr, const int32_t* left,
-                                                        const uint32_t* edge, const uint32_t* ps,
-                                                        const uint32_t* node_off, uint32_t* node_offsets, float mn,
-                                                        float rg, gtc_octnode* nodes, uint32_t capacity,
-                                                        uint32_t* status) {
+// One octree body: code g of the cloud described by ci.
+__device__ __forceinline__ void bt_octree_one(uint32_t g, uint4 ci, const uint32_t* codes, const uint8_t* prefix_n,
+                                              const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
+                                              const uint32_t* edge, const uint32_t* ps, float mn, float rg,
+                                              gtc_octnode* nodes, uint32_t capacity, uint32_t* status) {
   constexpr int A = KeyTraits<uint32_t>::A;
+  const uint32_t U0 = ci.x, k = g - U0, m = ci.y - U0 - 1, bias = ci.z, O = ci.w;
+  if (O >= capacity) {
+    if (k == 0) atomicOr(status, DEV_CAPACITY);
+    return;
+  }
+  if (m == 0) {
+    octree_root_only<uint32_t>(nodes + O, capacity - O, mn, rg, status);
+    return;
+  }
+  const int root_level = (prefix_n[U0] - A) / 3;
+  octree_make_node<uint32_t, true>(k, codes + U0, prefix_n + U0, hll + U0, hlr + U0, left + U0, edge + U0, ps + U0,
+                                   bias, root_level, mn, rg, nodes + O, capacity - O, status);
+}
+
+// Octree of every cloud, and the cloud-local node offsets (what the
+// single-cloud node-offset scan gives each cloud).  Warp slices of 32 codes:
+// the slice's cloud comes from one binary search (then a step or two per
+// lane), every lane writes its node offset, and the codes that own octree
+// nodes are compacted into a per-warp queue and processed 32 at a time, as in
+// octree.cu.
+__global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restrict__ codes, const uint32_t* uoff,
+                                                        uint32_t S, const uint4* cinfo, const uint8_t* prefix_n,
+                                                        const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
+                                                        const uint32_t* edge, const uint32_t* ps,
+                                                        uint32_t* node_offsets, float mn, float rg, gtc_octnode* nodes,
+                                                        uint32_t capacity, uint32_t* status) {
+  constexpr int WARPS = 256 / 32;
+  __shared__ uint2 s_queue[WARPS][64];
   const uint32_t U = uoff[S];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < U; g += stride) {
-    const uint32_t c = owner(uoff, S, g);
-    const uint32_t U0 = uoff[c];
-    const uint32_t k = g - U0;
-    const uint32_t m = uoff[c + 1] - U0 - 1;
-    const uint32_t bias = U0 > 0 ? ps[U0 - 1] : 0u;
-    node_offsets[g] = (k == 0) ? 0u : ps[g] - bias;
-    if (m > 0 && k >= m) continue;
-    const uint32_t O = node_off[c];
-    if (O >= capacity) {
-      if (k == 0) atomicOr(status, DEV_CAPACITY);
-      continue;
+  const int lane = threadIdx.x & 31;
+  uint2* q = s_queue[threadIdx.x >> 5];
+  uint32_t qn = 0;  // warp-uniform
+  const uint32_t warps = gridDim.x * WARPS;
+  for (uint32_t base = (blockIdx.x * WARPS + (threadIdx.x >> 5)) * 32; base < U; base += warps * 32) {
+    const uint32_t g = base + lane;
+    bool act = false;
+    uint32_t c = owner(uoff, S, base);  // the same address in every lane
+    if (g < U) {
+      while (g >= uoff[c + 1]) ++c;
+      const uint4 ci = cinfo[c];
+      const uint32_t k = g - ci.x, m = ci.y - ci.x - 1;
+      node_offsets[g] = (k == 0) ? 0u : ps[g] - ci.z;
+      act = (m == 0) ? true : (k < m && (k == 0 || edge[g] > 0));
     }
-    if (m == 0) {
-      octree_root_only<uint32_t>(nodes + O, capacity - O, mn, rg, status);
-      continue;
+    const uint32_t bal = __ballot_sync(0xffffffffu, act);
+    if (act) q[qn + __popc(bal & ((1u << lane) - 1u))] = make_uint2(g, c);
+    qn += __popc(bal);
+    __syncwarp();
+    if (qn >= 32) {
+      const uint2 e = q[lane];
+      bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, status);
+      const uint2 rest = (lane + 32 < qn) ? q[lane + 32] : make_uint2(0, 0);
+      __syncwarp();
+      if (lane + 32 < qn) q[lane] = rest;
+      qn -= 32;
+      __syncwarp();
     }
-    const int root_level = (prefix_n[U0] - A) / 3;
-    octree_make_node<uint32_t, true>(k, codes + U0, prefix_n + U0, hll + U0, hlr + U0, left + U0, edge + U0,
-                                     ps + U0, bias, root_level, mn, rg, nodes + O, capacity - O, status);
+  }
+  if (lane < qn) {
+    const uint2 e = q[lane];
+    bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, status);
   }
 }
 
@@ -615,16 +655,19 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   {
     Stage t(ctx, stream, GTC_STAGE_PREFIX_SUM);
     BCHK(launch_inclusive_scan_dev(L, out->edge_count, W.ps, out->key_offset + S, n_total, W.scan_ws));
+    // The per-cloud digit histograms are dead after the sort: their space
+    // holds the per-cloud octree info.
     bt_cloud_offsets_kernel<<<ceil_div(S, 256), 256, 0, s>>>(out->key_offset, W.ne_start, W.ps, S,
-                                                            out->node_offset, out->cloud_counts, bad);
+                                                            out->node_offset, out->cloud_counts,
+                                                            reinterpret_cast<uint4*>(W.seg_hist), bad);
     BCHK(cudaGetLastError());
   }
   {
     Stage t(ctx, stream, GTC_STAGE_OCTREE);
-    const uint32_t ogrid = max(1u, min(ceil_div(n_total, 256), (uint32_t)L.num_sms * 16));
-    bt_octree_kernel<<<ogrid, 256, 0, s>>>(out->keys, out->key_offset, S, out->prefix_n, out->has_leaf_left,
-                                           out->has_leaf_right, out->left_child, out->edge_count, W.ps,
-                                           out->node_offset, out->node_offsets, min_coord, range, out->nodes,
+    const uint32_t ogrid = max(1u, min(ceil_div(n_total, 256), (uint32_t)L.num_sms * 5));
+    bt_octree_kernel<<<ogrid, 256, 0, s>>>(out->keys, out->key_offset, S, reinterpret_cast<const uint4*>(W.seg_hist),
+                                           out->prefix_n, out->has_leaf_left, out->has_leaf_right, out->left_child,
+                                           out->edge_count, W.ps, out->node_offsets, min_coord, range, out->nodes,
                                            out->nodes_capacity, L.status);
     BCHK(cudaGetLastError());
   }

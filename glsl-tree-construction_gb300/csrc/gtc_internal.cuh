@@ -219,6 +219,34 @@ __device__ __forceinline__ float4 decode_corner(K code, float mn, float rg) {
   return r;
 }
 
+// 2^-k as a float, exact (0 <= k <= 126).
+__device__ __forceinline__ float exp2_neg(int k) { return __int_as_float((127 - k) << 23); }
+
+// Integer cell coordinates of a code: the decode of morton.rs:43-74 without
+// the scaling.
+template <class K>
+__device__ __forceinline__ uint3 code_xyz(K code) {
+  return make_uint3(third_bits(code), third_bits((K)(code >> 1)), third_bits((K)(code >> 2)));
+}
+
+// decode_corner of a code's prefix of `level` octants, from the code's cell
+// coordinates q: the prefix clears the low B - level bits of every axis.
+// Division by 2^B is the exact scaling by 2^-B in IEEE arithmetic (the same
+// correctly rounded value), so a multiplication by 2^-B gives decode_corner's
+// result bit for bit at a fraction of the cost.
+template <class K>
+__device__ __forceinline__ float4 corner_at(uint3 q, int level, float mn, float rg) {
+  constexpr int B = KeyTraits<K>::B;
+  const uint32_t m = ~((1u << (B - level)) - 1u);
+  const float s = exp2_neg(B);
+  float4 r;
+  r.x = __fadd_rn(__fmul_rn(__fmul_rn((float)(q.x & m), s), rg), mn);
+  r.y = __fadd_rn(__fmul_rn(__fmul_rn((float)(q.y & m), s), rg), mn);
+  r.z = __fadd_rn(__fmul_rn(__fmul_rn((float)(q.z & m), s), rg), mn);
+  r.w = 1.0f;
+  return r;
+}
+
 // ----------------------------------------------------------- warp scans ---
 __device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v) {
   const int lane = threadIdx.x & 31;

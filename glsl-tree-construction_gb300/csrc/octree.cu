@@ -8,8 +8,12 @@ namespace gtc {
 constexpr int OCT_THREADS = 256;
 
 // The kernel is bound by the latency of its dependent loads (node -> child ->
-// grandchild), not by bandwidth: one thread per radix node, no block barriers,
-// 16-byte stores straight to HBM.
+// grandchild), not by bandwidth.  Only about a third of the radix nodes own
+// octree nodes, so each warp first compacts the contributing nodes of
+// consecutive 32-node slices into a queue in shared memory (ballot + popc)
+// and runs the node body only on full batches of 32: every lane busy, 32
+// independent load chains in flight per warp.  No block barriers; 16-byte
+// stores straight to HBM.
 template <class K, bool WITH_LEAVES>
 __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __restrict__ codes, const uint32_t* d_u,
                                                                   uint32_t u_host, const uint8_t* __restrict__ prefix_n,
@@ -21,6 +25,8 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
                                                                   gtc_octnode* __restrict__ nodes, uint32_t capacity,
                                                                   uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
+  constexpr int WARPS = OCT_THREADS / 32;
+  __shared__ uint32_t s_queue[WARPS][64];
   const uint32_t u = d_u ? *d_u : u_host;
   if (u == 0) return;
   const uint32_t m = u - 1;
@@ -29,10 +35,30 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
     return;
   }
   const int root_level = (prefix_n[0] - A) / 3;
-  const uint32_t stride = gridDim.x * OCT_THREADS;
-  for (uint32_t k = blockIdx.x * OCT_THREADS + threadIdx.x; k < m; k += stride)
-    octree_make_node<K, WITH_LEAVES>(k, codes, prefix_n, hll, hlr, left, edge, ps, 0u, root_level, mn, rg, nodes,
-                                     capacity, status);
+  const int lane = threadIdx.x & 31;
+  uint32_t* q = s_queue[threadIdx.x >> 5];
+  uint32_t qn = 0;  // warp-uniform
+  const uint32_t warps = gridDim.x * WARPS;
+  for (uint32_t base = (blockIdx.x * WARPS + (threadIdx.x >> 5)) * 32; base < m; base += warps * 32) {
+    const uint32_t k = base + lane;
+    const bool act = k < m && (k == 0 || edge[k] > 0);
+    const uint32_t bal = __ballot_sync(0xffffffffu, act);
+    if (act) q[qn + __popc(bal & ((1u << lane) - 1u))] = k;
+    qn += __popc(bal);
+    __syncwarp();
+    if (qn >= 32) {
+      octree_make_node<K, WITH_LEAVES>(q[lane], codes, prefix_n, hll, hlr, left, edge, ps, 0u, root_level, mn, rg,
+                                       nodes, capacity, status);
+      const uint32_t rest = (lane + 32 < qn) ? q[lane + 32] : 0u;
+      __syncwarp();
+      if (lane + 32 < qn) q[lane] = rest;
+      qn -= 32;
+      __syncwarp();
+    }
+  }
+  if (lane < qn)
+    octree_make_node<K, WITH_LEAVES>(q[lane], codes, prefix_n, hll, hlr, left, edge, ps, 0u, root_level, mn, rg,
+                                     nodes, capacity, status);
 }
 
 template <class K>
@@ -42,7 +68,9 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
                                gtc_octnode* nodes, uint32_t capacity, bool with_leaves) {
   const uint32_t work = d_u ? n_max : u_host;
   if (work == 0) return cudaSuccess;
-  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 16));
+  // One resident wave (5 blocks of 256 per SM at 48 registers); each warp
+  // walks many 32-node slices, so the partial batch at its end is small.
+  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 5));
   if (with_leaves)
     octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
                                                                      edge, ps, mn, rg, nodes, capacity, L.status);

@@ -139,16 +139,19 @@ __device__ __forceinline__ void octree_make_node(uint32_t k, const K* __restrict
   int4 lo = make_int4(0, 0, 0, 0), hi = make_int4(0, 0, 0, 0);
   int32_t nmask = 0, lmask = 0;
   gather<K, WITH_LEAVES, 0>(k, dk + 1, codes, hll, hlr, left, edge, ps, ps_bias, lo, hi, nmask, lmask, status);
-  store_node(nodes, bottom, lo, hi, decode_corner<K>(level_prefix<K>(code_k, dk), mn, rg),
-             __fdiv_rn(rg, (float)(1u << (dk - root_level))), nmask, lmask);
+  // Corners from the cell coordinates decoded once; cell sizes rg / 2^k as
+  // the exact scaling rg * 2^-k (octree.comp:111-116, 181-182).
+  const uint3 q = code_xyz<K>(code_k);
+  store_node(nodes, bottom, lo, hi, corner_at<K>(q, dk, mn, rg), __fmul_rn(rg, exp2_neg(dk - root_level)), nmask,
+             lmask);
   // Chain nodes above the bottom (levels dk - 1 .. dk - c + 1).
   for (uint32_t j = 1; j < c; ++j) {
     const int level = dk - (int)j;
     int4 a = make_int4(0, 0, 0, 0), b = make_int4(0, 0, 0, 0);
     const int w = child_slot<K>(code_k, level + 1);
     set_child(a, b, w, (int32_t)(bottom + j - 1));
-    store_node(nodes, bottom + j, a, b, decode_corner<K>(level_prefix<K>(code_k, level), mn, rg),
-               __fdiv_rn(rg, (float)(1u << (level - root_level))), 1 << w, 0);
+    store_node(nodes, bottom + j, a, b, corner_at<K>(q, level, mn, rg), __fmul_rn(rg, exp2_neg(level - root_level)),
+               1 << w, 0);
   }
 }
 
