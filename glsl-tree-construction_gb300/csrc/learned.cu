@@ -13,13 +13,17 @@
 // heights are non-decreasing (the update projects them so).
 //
 // Sort (all stream-ordered, decisions on the device):
-//   1. count:   per 64K-key tile, B-bin shared histogram of model buckets;
-//   2. scan:    per-bucket offsets over tiles, bucket bases; a bucket larger
-//               than the on-chip capacity sets the OVERFLOW flag;
-//   3. scatter: each key (with its value and position) to its bucket segment;
+//   1. count:   the model bucket of every key, written as a u16 id, and the
+//               global bucket histogram;
+//   2. scan:    bucket bases; a bucket larger than the on-chip capacity sets
+//               the OVERFLOW flag, non-monotone heights BAD_MODEL;
+//   3. group:   two stable LSD passes over the bucket-id digits (onesweep
+//               style: tile-local ranking, decoupled look-back, coalesced
+//               runs of writes) carry keys and values into bucket order, equal
+//               keys still in input order;
 //   4. bucket sort: one CTA per bucket sorts its segment in shared memory
-//               (LSD over the bits that vary inside the bucket, then equal
-//               keys ordered by original position) and writes the output;
+//               (stable passes over the 16 highest bits that vary inside the
+//               bucket, then short groups by insertion) and writes the output;
 //   5. check:   consecutive non-empty buckets must hold increasing key ranges
 //               (ORDER flag);
 //   6. fallback: with any flag set, the input is copied to the output and the
@@ -39,14 +43,12 @@ gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_
 constexpr uint32_t LFLAG_OVERFLOW = 1u;   // a bucket exceeds the on-chip sort capacity
 constexpr uint32_t LFLAG_ORDER = 2u;      // bucket key ranges out of order
 constexpr uint32_t LFLAG_BAD_MODEL = 4u;  // heights not non-decreasing
-constexpr uint32_t LFLAG_DUP_RUN = 8u;    // a run of equal keys too long to order on chip
 
 constexpr int LC_THREADS = 1024;
 constexpr int LC_KPT = 64;
 constexpr int LC_TILE = LC_THREADS * LC_KPT;  // 65536 keys per count/scatter tile
 constexpr int BS_THREADS = 1024;
 constexpr int BS_CAP = 16384;                 // keys per bucket sorted on chip (229,920 B of smem)
-constexpr int BS_MAX_RUN = 256;
 constexpr int MAX_BUCKETS = 8192;  // knots + heights + histogram must fit one CTA's shared memory
 
 // ---------------------------------------------------------------- model ---
@@ -205,10 +207,18 @@ __global__ void __launch_bounds__(1024) adam_kernel(float* y, const float* grad,
 }
 
 // --------------------------------------------------------------- sorting --
-struct ModelSmem {
-  uint64_t* kn;
-  float* y;
-};
+// Per-key bucket ids are computed once (count pass) and carried as a u16
+// payload through two stable LSD passes over their digits, which group the
+// keys by bucket with tile-local ranking and coalesced runs of writes (the
+// onesweep pass of sort.cu with a third array).  Stable passes keep equal
+// keys in input order inside every bucket, so the in-bucket sort needs no
+// positions to order them.
+constexpr int LP_THREADS = 256;
+constexpr int LP_KPT = 16;
+constexpr int LP_TILE = LP_THREADS * LP_KPT;  // 4096 keys per pass tile
+constexpr int LP_RADIX = 128;                 // bucket-id digits of at most 7 bits
+constexpr int LP_WARPS = LP_THREADS / 32;
+constexpr int BS_GROUP = 32;                  // longest equal-prefix group finished by insertion
 
 __device__ __forceinline__ void load_model(uint64_t* s_kn, float* s_y, const uint64_t* kn, const float* y, int B) {
   for (int i = threadIdx.x; i <= B; i += blockDim.x) {
@@ -217,9 +227,11 @@ __device__ __forceinline__ void load_model(uint64_t* s_kn, float* s_y, const uin
   }
 }
 
+// 1. bucket of every key (written as u16 when bids is set) and the global
+// bucket histogram (one atomic per non-empty bucket and tile).
 __global__ void __launch_bounds__(LC_THREADS) learned_count_kernel(const uint64_t* __restrict__ keys, uint32_t n,
                                                                    const uint64_t* kn, const float* y, int B,
-                                                                   uint32_t* counts) {
+                                                                   uint32_t* totals, uint16_t* __restrict__ bids) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
   uint64_t* s_kn = s_e + B;
@@ -233,108 +245,300 @@ __global__ void __launch_bounds__(LC_THREADS) learned_count_kernel(const uint64_
 #pragma unroll 4
   for (int j = 0; j < LC_KPT; ++j) {
     const size_t i = base + (size_t)j * LC_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&s_hist[model_bucket(__ldcs(keys + i), s_e, s_kn, s_y, B)], 1u);
-  }
-  __syncthreads();
-  for (int b = threadIdx.x; b < B; b += LC_THREADS) counts[(size_t)blockIdx.x * B + b] = s_hist[b];
-}
-
-// Thread per bucket: exclusive offsets over tiles (in place), totals and the
-// capacity check; the last block scans the totals into bucket bases.
-__global__ void __launch_bounds__(1024) learned_scan_kernel(uint32_t* counts, uint32_t tiles, int B, const float* y,
-                                                            uint32_t* totals, uint32_t* base, uint32_t* flags,
-                                                            uint32_t* done) {
-  __shared__ uint32_t s_part[1024];
-  __shared__ uint32_t s_last;
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < B) {
-    uint32_t run = 0;
-    for (uint32_t t = 0; t < tiles; ++t) {
-      const uint32_t c = counts[(size_t)t * B + b];
-      counts[(size_t)t * B + b] = run;
-      run += c;
-    }
-    totals[b] = run;
-    if (run > (uint32_t)BS_CAP) atomicOr(flags, LFLAG_OVERFLOW);
-    if (y[b] > y[b + 1]) atomicOr(flags, LFLAG_BAD_MODEL);
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1) ? 1u : 0u;
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  const int per = (B + 1023) / 1024;
-  const int first = threadIdx.x * per;
-  uint32_t sum = 0;
-  for (int i = first; i < min(first + per, B); ++i) sum += __ldcg(totals + i);
-  s_part[threadIdx.x] = sum;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan of the chunk sums
-    const uint32_t t = (threadIdx.x >= (unsigned)o) ? s_part[threadIdx.x - o] : 0u;
-    __syncthreads();
-    s_part[threadIdx.x] += t;
-    __syncthreads();
-  }
-  uint32_t run = threadIdx.x > 0 ? s_part[threadIdx.x - 1] : 0u;
-  for (int i = first; i < min(first + per, B); ++i) {
-    base[i] = run;
-    run += __ldcg(totals + i);
-  }
-  if (threadIdx.x == 0) *done = 0;
-}
-
-__global__ void __launch_bounds__(LC_THREADS) learned_scatter_kernel(
-    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n, const uint64_t* kn,
-    const float* y, int B, const uint32_t* counts, const uint32_t* base, uint64_t* __restrict__ tkeys,
-    uint32_t* __restrict__ tvals, uint32_t* __restrict__ tpos, const uint32_t* flags) {
-  if (*flags) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
-  uint64_t* s_kn = s_e + B;
-  float* s_y = reinterpret_cast<float*>(s_kn + (B + 1));
-  uint32_t* s_off = reinterpret_cast<uint32_t*>(s_y + (B + 1));
-  load_model(s_kn, s_y, kn, y, B);
-  build_eytzinger(s_e, kn, B);
-  for (int b = threadIdx.x; b < B; b += LC_THREADS) s_off[b] = base[b] + counts[(size_t)blockIdx.x * B + b];
-  __syncthreads();
-  const size_t tile0 = (size_t)blockIdx.x * LC_TILE;
-#pragma unroll 4
-  for (int j = 0; j < LC_KPT; ++j) {
-    const size_t i = tile0 + (size_t)j * LC_THREADS + threadIdx.x;
     if (i < n) {
-      const uint64_t k = __ldcs(keys + i);
-      const uint32_t r = atomicAdd(&s_off[model_bucket(k, s_e, s_kn, s_y, B)], 1u);
-      tkeys[r] = k;
-      tvals[r] = vals ? __ldcs(vals + i) : (uint32_t)i;
-      tpos[r] = (uint32_t)i;
+      const int b = model_bucket(__ldcs(keys + i), s_e, s_kn, s_y, B);
+      atomicAdd(&s_hist[b], 1u);
+      if (bids) bids[i] = (uint16_t)b;
     }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += LC_THREADS) {
+    const uint32_t c = s_hist[b];
+    if (c) atomicAdd(totals + b, c);
   }
 }
 
+// 2. one block: bucket bases, the capacity and model checks, and the digit
+// bases of the two passes (low db1 bits of the bucket id, then the rest).
+__global__ void __launch_bounds__(1024) learned_scan_kernel(const uint32_t* totals, int B, int db1, const float* y,
+                                                            uint32_t* base, uint32_t* off1, uint32_t* off2,
+                                                            uint32_t* flags) {
+  __shared__ uint32_t s_part[1024];
+  const int tid = threadIdx.x;
+  const int per = (B + 1023) / 1024;
+  const int first = tid * per, last = min(first + per, B);
+  uint32_t sum = 0;
+  bool over = false, bad = false;
+  for (int i = first; i < last; ++i) {
+    const uint32_t t = totals[i];
+    sum += t;
+    over |= t > (uint32_t)BS_CAP;
+    bad |= y[i] > y[i + 1];
+  }
+  if (over) atomicOr(flags, LFLAG_OVERFLOW);
+  if (bad) atomicOr(flags, LFLAG_BAD_MODEL);
+  s_part[tid] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const uint32_t t = (tid >= o) ? s_part[tid - o] : 0u;
+    __syncthreads();
+    s_part[tid] += t;
+    __syncthreads();
+  }
+  uint32_t run = tid > 0 ? s_part[tid - 1] : 0u;
+  for (int i = first; i < last; ++i) {
+    base[i] = run;
+    run += totals[i];
+  }
+  __syncthreads();
+  const int r1 = 1 << db1;
+  if (tid < r1) {
+    uint32_t c = 0;
+    for (int b = tid; b < B; b += r1) c += totals[b];
+    s_part[tid] = c;
+  }
+  __syncthreads();
+  if (tid < r1) {
+    uint32_t pre = 0;
+    for (int d = 0; d < tid; ++d) pre += s_part[d];
+    off1[tid] = pre;
+  }
+  if (tid < (B >> db1)) off2[tid] = base[tid << db1];
+}
+
+// 3. one stable pass over the bucket-id digit (bid >> shift) & mask.  FIRST:
+// the caller's keys and values (values absent: the index) in, bucket ids
+// carried out; otherwise the ids are read and dropped.
+struct LpSmem {
+  uint64_t keys[LP_TILE];
+  uint32_t vals[LP_TILE];
+  uint16_t bids[LP_TILE];
+  uint32_t warp_hist[LP_WARPS][LP_RADIX];
+  uint32_t gbase[LP_RADIX];
+  uint32_t warp_sums[LP_RADIX / 32];
+  uint32_t tile_id;
+};
+
+template <bool FIRST>
+__global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, const uint16_t* __restrict__ bin,
+    uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint16_t* __restrict__ bout, uint32_t n, int shift,
+    uint32_t mask, const uint32_t* __restrict__ bin_off, uint32_t* __restrict__ desc, uint32_t* tile_counter,
+    uint32_t* status, const uint32_t* flags) {
+  if (*flags & (LFLAG_OVERFLOW | LFLAG_BAD_MODEL)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LpSmem& s = *reinterpret_cast<LpSmem*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int i = tid; i < LP_WARPS * LP_RADIX; i += LP_THREADS) (&s.warp_hist[0][0])[i] = 0;
+  if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s.tile_id;
+  const uint32_t tbase = tile * LP_TILE;
+
+  uint64_t key[LP_KPT];
+  uint32_t val[LP_KPT], bd[LP_KPT];
+  const uint32_t wbase = tbase + warp * 32 * LP_KPT + lane;
+#pragma unroll
+  for (int j = 0; j < LP_KPT; ++j) {
+    const uint32_t pos = wbase + j * 32;
+    const bool ok = pos < n;
+    key[j] = ok ? kin[pos] : ~0ull;
+    val[j] = ok ? ((FIRST && !vin) ? pos : vin[pos]) : 0u;
+    bd[j] = ok ? (uint32_t)bin[pos] : 0xffffu;  // padding ranks last
+  }
+  uint32_t* my_hist = s.warp_hist[warp];
+#pragma unroll
+  for (int j = 0; j < LP_KPT; ++j) {
+    const uint32_t d = (bd[j] >> shift) & mask;
+    const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+    if (__all_sync(0xffffffffu, d == d0)) {
+      if (lane == 0) atomicAdd(&my_hist[d], 32u);
+    } else {
+      atomicAdd(&my_hist[d], 1u);
+    }
+  }
+  __syncthreads();
+  uint32_t count = 0;
+  if (tid < LP_RADIX) {
+#pragma unroll
+    for (int w = 0; w < LP_WARPS; ++w) {
+      const uint32_t c = s.warp_hist[w][tid];
+      s.warp_hist[w][tid] = count;
+      count += c;
+    }
+    st_relaxed(desc + (size_t)tile * LP_RADIX + tid, (count << 2) | (tile == 0 ? FLAG_INCLUSIVE : FLAG_AGGREGATE));
+  }
+  uint32_t incl = 0;
+  if (tid < LP_RADIX) {
+    incl = warp_inclusive_sum(count);
+    if (lane == 31) s.warp_sums[warp] = incl;
+  }
+  __syncthreads();
+  uint32_t doff = 0;
+  if (tid < LP_RADIX) {
+    for (int w = 0; w < LP_RADIX / 32; ++w) doff += (w < warp) ? s.warp_sums[w] : 0u;
+    doff += incl - count;
+#pragma unroll
+    for (int w = 0; w < LP_WARPS; ++w) s.warp_hist[w][tid] += doff;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < LP_KPT; ++j) {
+    const uint32_t d = (bd[j] >> shift) & mask;
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 7; ++b) {
+      const uint32_t bit = (d >> b) & 1u;
+      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? bal : ~bal;
+    }
+    const int leader = 31 - __clz(peers);
+    uint32_t b0 = 0;
+    if (lane == leader) b0 = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
+    b0 = __shfl_sync(0xffffffffu, b0, leader);
+    const uint32_t local = b0 + __popc(peers & lt_mask);
+    s.keys[local] = key[j];
+    s.vals[local] = val[j];
+    s.bids[local] = (uint16_t)bd[j];
+  }
+  if (tid < LP_RADIX) {
+    uint32_t excl = 0;
+    if (tile > 0) {
+      excl = lookback_window<8, LP_RADIX>(desc, tile, tid, status);
+      st_relaxed(desc + (size_t)tile * LP_RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
+    }
+    s.gbase[tid] = bin_off[tid] + excl - doff;
+  }
+  __syncthreads();
+  const uint32_t valid = min((uint32_t)LP_TILE, n - tbase);
+  for (uint32_t i = tid; i < valid; i += LP_THREADS) {
+    const uint32_t b = s.bids[i];
+    const uint32_t o = s.gbase[(b >> shift) & mask] + i;
+    kout[o] = s.keys[i];
+    vout[o] = s.vals[i];
+    if (FIRST) bout[o] = (uint16_t)b;
+  }
+}
+
+// 4. in-bucket sort.
 struct BucketSmem {
   uint64_t keys[BS_CAP];
   uint16_t idx[2][BS_CAP];
   uint32_t hist[BS_THREADS / 32][256];
   uint32_t warp_sums[8];
   uint64_t red[64];
-  uint32_t skip;
+  uint32_t skip, big;
 };
 
-// One CTA per bucket: LSD counting sort (8-bit digits) of the bucket's key
-// indices in shared memory over the bits that vary inside the bucket, then
-// runs of equal keys ordered by original position, then the output.
+// One stable 8-bit counting pass of the index array idx[cur] by the digit
+// (key >> shift) & 255, into idx[cur ^ 1] (cur flips), unless every key has
+// the same digit.  Warp w owns positions [w * 32 * ipt, (w + 1) * 32 * ipt).
+// Called by every thread of the block.
+__device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt, int shift, int& cur) {
+  constexpr int WARPS = BS_THREADS / 32;
+  constexpr int IPT = BS_CAP / BS_THREADS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t wrun = (uint32_t)warp * 32u * (uint32_t)ipt;
+  for (int i = tid; i < WARPS * 256; i += BS_THREADS) (&s.hist[0][0])[i] = 0;
+  if (tid == 0) s.skip = 0;
+  __syncthreads();
+  // A. per-warp digit counts over this warp's run of positions.
+  uint32_t d[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; ++j) {
+    d[j] = 256u;
+    if (j < ipt) {
+      const uint32_t pos = wrun + j * 32 + lane;
+      if (pos < cnt) d[j] = (uint32_t)(s.keys[s.idx[cur][pos]] >> shift) & 255u;
+      if (d[j] < 256u) atomicAdd(&s.hist[warp][d[j]], 1u);
+    }
+  }
+  __syncthreads();
+  // B. warp offsets per digit and digit bases: thread (digit dg, group g)
+  // scans warps 8g..8g+7 of its digit; the four group sums are combined per
+  // digit (scratch: the index array phase C writes, unused until then).
+  uint32_t* gs = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]);
+  const int dg = tid & 255, grp = tid >> 8;
+  uint32_t part = 0;
+#pragma unroll
+  for (int w = 8 * grp; w < 8 * grp + 8; ++w) {
+    const uint32_t c = s.hist[w][dg];
+    s.hist[w][dg] = part;
+    part += c;
+  }
+  gs[grp * 256 + dg] = part;
+  __syncthreads();
+  uint32_t count = 0;
+  if (tid < 256) {
+    count = gs[tid] + gs[256 + tid] + gs[512 + tid] + gs[768 + tid];
+    if (count == cnt) s.skip = 1;  // every key has this digit: the pass is the identity
+  }
+  uint32_t incl = 0;
+  if (tid < 256) {
+    incl = warp_inclusive_sum(count);
+    if (lane == 31) s.warp_sums[warp] = incl;
+  }
+  __syncthreads();
+  if (tid < 256) {
+    uint32_t pre = 0;
+    for (int w = 0; w < 8; ++w) pre += (w < warp) ? s.warp_sums[w] : 0u;
+    uint32_t run = pre + incl - count;  // digit base
+    for (int g = 0; g < 4; ++g) {
+      const uint32_t t = gs[g * 256 + tid];
+      gs[g * 256 + tid] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  {
+    const uint32_t goff = gs[grp * 256 + dg];
+#pragma unroll
+    for (int w = 8 * grp; w < 8 * grp + 8; ++w) s.hist[w][dg] += goff;
+  }
+  __syncthreads();
+  if (s.skip) return;  // block-uniform
+  // C. stable ranks (peer masks over valid lanes) and the scatter of indices.
+#pragma unroll
+  for (int j = 0; j < IPT; ++j) {
+    if (j >= ipt || wrun + j * 32 >= cnt) break;  // warp-uniform
+    const uint32_t pos = wrun + j * 32 + lane;
+    const bool valid = d[j] < 256u;
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+      const uint32_t x = (d[j] >> bit) & 1u;
+      const uint32_t bal = __ballot_sync(0xffffffffu, x);
+      peers &= x ? bal : ~bal;
+    }
+    const int leader = valid ? 31 - __clz(peers) : 0;
+    uint32_t b0 = 0;
+    if (valid && lane == leader) b0 = atomicAdd(&s.hist[warp][d[j]], (uint32_t)__popc(peers));
+    b0 = __shfl_sync(0xffffffffu, b0, leader);
+    if (valid) s.idx[cur ^ 1][b0 + __popc(peers & lt_mask)] = s.idx[cur][pos];
+  }
+  __syncthreads();
+  cur ^= 1;
+}
+
+// One CTA per bucket (its keys arrive grouped and in input order).  Stable
+// sort in shared memory by the 16 highest bits that vary inside the bucket
+// (two 8-bit passes), then every group of keys equal in those bits (short:
+// the model spreads a bucket's keys) finished by a stable insertion sort on
+// the full key.  A bucket with a longer group (measured on the 64M config-5
+// keys: 7.5% of buckets; a 12-bit unstable binning pass instead left a
+// quarter of the buckets with a crowded bin) is re-sorted by full passes over
+// all its varying bits.
 __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
-    const uint64_t* __restrict__ tkeys, const uint32_t* __restrict__ tvals, const uint32_t* __restrict__ tpos,
-    const uint32_t* base, const uint32_t* totals, uint64_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
-    uint64_t* bmin, uint64_t* bmax, uint32_t* flags) {
+    const uint64_t* __restrict__ ukeys, const uint32_t* __restrict__ uvals, const uint32_t* base,
+    const uint32_t* totals, uint64_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals, uint64_t* bmin,
+    uint64_t* bmax, uint32_t* flags) {
   if (*flags & (LFLAG_OVERFLOW | LFLAG_BAD_MODEL)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BucketSmem& s = *reinterpret_cast<BucketSmem*>(smem_raw);
   constexpr int WARPS = BS_THREADS / 32;
-  constexpr int IPT = BS_CAP / BS_THREADS;  // 12 positions per thread
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t lt_mask = (1u << lane) - 1u;
   const int b = blockIdx.x;
   const uint32_t cnt = totals[b];
   const uint32_t off = base[b];
@@ -345,13 +549,13 @@ __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
     }
     return;
   }
-  if (cnt > (uint32_t)BS_CAP) {
+  if (cnt > (uint32_t)BS_CAP) {  // the scan has flagged it already
     if (tid == 0) atomicOr(flags, LFLAG_OVERFLOW);
     return;
   }
   uint64_t mn = ~0ull, mx = 0;
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-    const uint64_t k = tkeys[off + i];
+    const uint64_t k = ukeys[off + i];
     s.keys[i] = k;
     s.idx[0][i] = (uint16_t)i;
     mn = min(mn, k);
@@ -366,6 +570,7 @@ __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
     s.red[warp] = mn;
     s.red[32 + warp] = mx;
   }
+  if (tid == 0) s.big = 0;
   __syncthreads();
   mn = s.red[0];
   mx = s.red[32];
@@ -374,124 +579,45 @@ __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
     mx = max(mx, s.red[32 + w]);
   }
   const int vbits = (mn == mx) ? 0 : 64 - __clzll((long long)(mn ^ mx));
-  const int passes = (vbits + 7) / 8;
-  // Positions per thread for this bucket: warp w owns the contiguous run
-  // [w * 32 * ipt, (w + 1) * 32 * ipt), so ranks stay stable and no thread
-  // loops over the empty tail of a small bucket.
   const int ipt = (int)((cnt + BS_THREADS - 1) / BS_THREADS);
-  const uint32_t wrun = (uint32_t)warp * 32u * (uint32_t)ipt;
   int cur = 0;
-  for (int p = 0; p < passes; ++p) {
-    const int shift = 8 * p;
-    for (int i = tid; i < WARPS * 256; i += BS_THREADS) (&s.hist[0][0])[i] = 0;
-    if (tid == 0) s.skip = 0;
-    __syncthreads();
-    // A. per-warp digit counts over this warp's run of positions.
-    uint32_t d[IPT];
-#pragma unroll
-    for (int j = 0; j < IPT; ++j) {
-      d[j] = 256u;
-      if (j < ipt) {
-        const uint32_t pos = wrun + j * 32 + lane;
-        if (pos < cnt) d[j] = (uint32_t)(s.keys[s.idx[cur][pos]] >> shift) & 255u;
-        if (d[j] < 256u) atomicAdd(&s.hist[warp][d[j]], 1u);
-      }
-    }
-    __syncthreads();
-    // B. warp offsets per digit and digit bases: thread (digit dg, group g)
-    // scans warps 8g..8g+7 of its digit; the four group sums are combined per
-    // digit (scratch: the index array phase C writes, unused until then).
-    uint32_t* gs = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]);
-    const int dg = tid & 255, grp = tid >> 8;
-    uint32_t part = 0;
-#pragma unroll
-    for (int w = 8 * grp; w < 8 * grp + 8; ++w) {
-      const uint32_t c = s.hist[w][dg];
-      s.hist[w][dg] = part;
-      part += c;
-    }
-    gs[grp * 256 + dg] = part;
-    __syncthreads();
-    uint32_t count = 0;
-    if (tid < 256) {
-      count = gs[tid] + gs[256 + tid] + gs[512 + tid] + gs[768 + tid];
-      if (count == cnt) s.skip = 1;  // every key has this digit: the pass is the identity
-    }
-    uint32_t incl = 0;
-    if (tid < 256) {
-      incl = warp_inclusive_sum(count);
-      if (lane == 31) s.warp_sums[warp] = incl;
-    }
-    __syncthreads();
-    if (tid < 256) {
-      uint32_t pre = 0;
-      for (int w = 0; w < 8; ++w) pre += (w < warp) ? s.warp_sums[w] : 0u;
-      uint32_t run = pre + incl - count;  // digit base
-      for (int g = 0; g < 4; ++g) {
-        const uint32_t t = gs[g * 256 + tid];
-        gs[g * 256 + tid] = run;
-        run += t;
-      }
-    }
-    __syncthreads();
-    {
-      const uint32_t goff = gs[grp * 256 + dg];
-#pragma unroll
-      for (int w = 8 * grp; w < 8 * grp + 8; ++w) s.hist[w][dg] += goff;
-    }
-    __syncthreads();
-    if (s.skip) continue;  // block-uniform
-    // C. stable ranks (peer masks over valid lanes) and the scatter of indices.
-#pragma unroll
-    for (int j = 0; j < IPT; ++j) {
-      if (j >= ipt || wrun + j * 32 >= cnt) break;  // warp-uniform
-      const uint32_t pos = wrun + j * 32 + lane;
-      const bool valid = d[j] < 256u;
-      uint32_t peers = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-      for (int bit = 0; bit < 8; ++bit) {
-        const uint32_t x = (d[j] >> bit) & 1u;
-        const uint32_t bal = __ballot_sync(0xffffffffu, x);
-        peers &= x ? bal : ~bal;
-      }
-      const int leader = valid ? 31 - __clz(peers) : 0;
-      uint32_t b0 = 0;
-      if (valid && lane == leader) b0 = atomicAdd(&s.hist[warp][d[j]], (uint32_t)__popc(peers));
-      b0 = __shfl_sync(0xffffffffu, b0, leader);
-      if (valid) s.idx[cur ^ 1][b0 + __popc(peers & lt_mask)] = s.idx[cur][pos];
-    }
-    __syncthreads();
-    cur ^= 1;
-  }
-  // Runs of equal keys: order by original position (insertion sort; runs are
-  // short for Morton codes of distinct points, long runs take the fallback).
-  for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-    const uint64_t k = s.keys[s.idx[cur][i]];
-    if (i > 0 && s.keys[s.idx[cur][i - 1]] == k) continue;  // not a run start
-    uint32_t e = i + 1;
-    while (e < cnt && s.keys[s.idx[cur][e]] == k) ++e;
-    if (e - i > 1) {
-      if (e - i > (uint32_t)BS_MAX_RUN) {
-        atomicOr(flags, LFLAG_DUP_RUN);
+  if (vbits <= 16) {
+    for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
+  } else {
+    const int lo = vbits - 16;
+    bucket_pass(s, cnt, ipt, lo, cur);
+    bucket_pass(s, cnt, ipt, lo + 8, cur);
+    for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+      const uint64_t h = s.keys[s.idx[cur][i]] >> lo;
+      if (i > 0 && (s.keys[s.idx[cur][i - 1]] >> lo) == h) continue;  // not a group start
+      uint32_t e = i + 1;
+      while (e < cnt && e - i <= (uint32_t)BS_GROUP && (s.keys[s.idx[cur][e]] >> lo) == h) ++e;
+      if (e - i > (uint32_t)BS_GROUP) {
+        s.big = 1;
         continue;
       }
-      for (uint32_t a = i + 1; a < e; ++a) {
+      for (uint32_t a = i + 1; a < e; ++a) {  // stable: strict comparison
         const uint16_t x = s.idx[cur][a];
-        const uint32_t px = tpos[off + x];
+        const uint64_t kx = s.keys[x];
         uint32_t c = a;
-        while (c > i && tpos[off + s.idx[cur][c - 1]] > px) {
+        while (c > i && s.keys[s.idx[cur][c - 1]] > kx) {
           s.idx[cur][c] = s.idx[cur][c - 1];
           --c;
         }
         s.idx[cur][c] = x;
       }
     }
+    __syncthreads();
+    if (s.big) {  // block-uniform: start over with full passes
+      for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[cur][i] = (uint16_t)i;
+      __syncthreads();
+      for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
+    }
   }
-  __syncthreads();
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
     const uint16_t x = s.idx[cur][i];
     out_keys[off + i] = s.keys[x];
-    out_vals[off + i] = tvals[off + x];
+    out_vals[off + i] = uvals[off + x];
   }
   if (tid == 0) {
     bmin[b] = mn;
@@ -521,31 +647,28 @@ __global__ void cond_copy_kernel(const uint64_t* keys, const uint32_t* vals, uin
   }
 }
 
-// Sum of per-tile histograms (diagnostic entry gtc_learned_histogram_u64).
-__global__ void sum_tiles_kernel(const uint32_t* c, uint32_t tiles, int B, uint32_t* out) {
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
-    uint32_t t = 0;
-    for (uint32_t i = 0; i < tiles; ++i) t += c[(size_t)i * B + b];
-    out[b] = t;
-  }
-}
-
 // ------------------------------------------------------------ host side --
 struct LearnedWorkspace {
-  uint32_t* counts;   // [tiles][B]
   uint32_t* totals;   // [B]
   uint32_t* base;     // [B]
   uint64_t* bmin;     // [B]
   uint64_t* bmax;     // [B]
-  uint32_t* misc;     // [0] done counter
-  uint64_t* tkeys;    // [n]
+  uint32_t* misc;     // [1], [2]: pass tile tickets
+  uint32_t* off1;     // [128] digit bases of pass 1
+  uint32_t* off2;     // [128] digit bases of pass 2
+  uint16_t* bid;      // [n] bucket ids
+  uint16_t* bid2;     // [n] bucket ids after pass 1
+  uint64_t* tkeys;    // [n] after pass 1 (and the fallback's alternate buffer)
   uint32_t* tvals;    // [n]
-  uint32_t* tpos;     // [n]
+  uint64_t* ukeys;    // [n] grouped by bucket
+  uint32_t* uvals;    // [n]
+  uint32_t* desc;     // [2][pass tiles][128]
+  size_t desc_words;  // per pass
   void* sort_ws;      // onesweep fallback workspace
 };
 
 static size_t learned_ws_layout(uint32_t n, int B, LearnedWorkspace* W, char* p) {
-  const uint32_t tiles = ceil_div(n > 0 ? n : 1, LC_TILE);
+  const uint32_t ptiles = ceil_div(n > 0 ? n : 1, LP_TILE);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     char* q = p ? p + o : nullptr;
@@ -553,15 +676,21 @@ static size_t learned_ws_layout(uint32_t n, int B, LearnedWorkspace* W, char* p)
     return q;
   };
   LearnedWorkspace w;
-  w.counts = reinterpret_cast<uint32_t*>(take((size_t)tiles * B * 4));
   w.totals = reinterpret_cast<uint32_t*>(take((size_t)B * 4));
   w.base = reinterpret_cast<uint32_t*>(take((size_t)B * 4));
   w.bmin = reinterpret_cast<uint64_t*>(take((size_t)B * 8));
   w.bmax = reinterpret_cast<uint64_t*>(take((size_t)B * 8));
   w.misc = reinterpret_cast<uint32_t*>(take(256));
+  w.off1 = reinterpret_cast<uint32_t*>(take(LP_RADIX * 4));
+  w.off2 = reinterpret_cast<uint32_t*>(take(LP_RADIX * 4));
+  w.bid = reinterpret_cast<uint16_t*>(take((size_t)n * 2));
+  w.bid2 = reinterpret_cast<uint16_t*>(take((size_t)n * 2));
   w.tkeys = reinterpret_cast<uint64_t*>(take((size_t)n * 8));
   w.tvals = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
-  w.tpos = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  w.ukeys = reinterpret_cast<uint64_t*>(take((size_t)n * 8));
+  w.uvals = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  w.desc_words = (size_t)ptiles * LP_RADIX;
+  w.desc = reinterpret_cast<uint32_t*>(take(2 * w.desc_words * 4));
   w.sort_ws = take(sort_workspace_bytes(n, 8, 0));
   if (W) *W = w;
   return o;
@@ -715,17 +844,13 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
   if (!ctx || !m || !d_counts || (n && !keys)) return GTC_ERR_INVALID_ARG;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int B = m->B;
-  const uint32_t tiles = ceil_div(n > 0 ? n : 1, LC_TILE);
-  uint32_t* counts = nullptr;
-  LTRY(ctx, cudaMallocAsync(reinterpret_cast<void**>(&counts), (size_t)tiles * B * 4, s));
-  const size_t smem = model_smem_bytes(B);
+  LTRY(ctx, cudaMemsetAsync(d_counts, 0, (size_t)B * 4, s));
+  if (n == 0) return GTC_OK;
   LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)model_smem_bytes(MAX_BUCKETS)));
-  learned_count_kernel<<<tiles, LC_THREADS, smem, s>>>(keys, n, m->knots, m->heights, B, counts);
+  learned_count_kernel<<<ceil_div(n, LC_TILE), LC_THREADS, model_smem_bytes(B), s>>>(keys, n, m->knots, m->heights, B,
+                                                                                     d_counts, nullptr);
   LTRY(ctx, cudaGetLastError());
-  sum_tiles_kernel<<<ceil_div(B, 256), 256, 0, s>>>(counts, tiles, B, d_counts);
-  LTRY(ctx, cudaGetLastError());
-  LTRY(ctx, cudaFreeAsync(counts, s));
   return GTC_OK;
 }
 
@@ -749,30 +874,42 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
   LearnedWorkspace W;
   learned_ws_layout(n, B, &W, reinterpret_cast<char*>(ws));
   const uint32_t tiles = ceil_div(n, LC_TILE);
+  const uint32_t ptiles = ceil_div(n, LP_TILE);
   const size_t msmem = model_smem_bytes(B);
+  const int lb = 31 - __builtin_clz((unsigned)B);  // bucket-id bits
+  const int db1 = (lb + 1) / 2, db2 = lb - db1;      // digit widths of the two passes (<= 7 each)
   static bool attr = false;
   if (!attr) {
     LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)model_smem_bytes(MAX_BUCKETS)));
-    LTRY(ctx, cudaFuncSetAttribute(learned_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)model_smem_bytes(MAX_BUCKETS)));
+    LTRY(ctx, cudaFuncSetAttribute(learned_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(LpSmem)));
+    LTRY(ctx, cudaFuncSetAttribute(learned_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(LpSmem)));
     LTRY(ctx, cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sizeof(BucketSmem)));
     attr = true;
   }
+  const Launch L0 = context_launch(ctx, stream);
   LTRY(ctx, cudaMemsetAsync(W.misc, 0, 256, s));
-  learned_count_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, n, m->knots, m->heights, B, W.counts);
-  learned_scan_kernel<<<ceil_div(B, 1024), 1024, 0, s>>>(W.counts, tiles, B, m->heights, W.totals, W.base, d_flags,
-                                                        W.misc);
-  learned_scatter_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, vals, n, m->knots, m->heights, B, W.counts, W.base,
-                                                         W.tkeys, W.tvals, W.tpos, d_flags);
-  bucket_sort_kernel<<<B, BS_THREADS, sizeof(BucketSmem), s>>>(W.tkeys, W.tvals, W.tpos, W.base, W.totals, keys_out,
-                                                               vals_out, W.bmin, W.bmax, d_flags);
+  LTRY(ctx, cudaMemsetAsync(W.totals, 0, (size_t)B * 4, s));
+  LTRY(ctx, cudaMemsetAsync(W.desc, 0, 2 * W.desc_words * 4, s));
+  learned_count_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, n, m->knots, m->heights, B, W.totals, W.bid);
+  learned_scan_kernel<<<1, 1024, 0, s>>>(W.totals, B, db1, m->heights, W.base, W.off1, W.off2, d_flags);
+  learned_pass_kernel<true><<<ptiles, LP_THREADS, sizeof(LpSmem), s>>>(
+      keys, vals, W.bid, db2 ? W.tkeys : W.ukeys, db2 ? W.tvals : W.uvals, W.bid2, n, 0, (1u << db1) - 1, W.off1,
+      W.desc, W.misc + 1, L0.status, d_flags);
+  if (db2)
+    learned_pass_kernel<false><<<ptiles, LP_THREADS, sizeof(LpSmem), s>>>(
+        W.tkeys, W.tvals, W.bid2, W.ukeys, W.uvals, nullptr, n, db1, (1u << db2) - 1, W.off2, W.desc + W.desc_words,
+        W.misc + 2, L0.status, d_flags);
+  bucket_sort_kernel<<<B, BS_THREADS, sizeof(BucketSmem), s>>>(W.ukeys, W.uvals, W.base, W.totals, keys_out, vals_out,
+                                                               W.bmin, W.bmax, d_flags);
   learned_order_check_kernel<<<ceil_div(B, 256), 256, 0, s>>>(W.totals, W.bmin, W.bmax, B, d_flags);
   LTRY(ctx, cudaGetLastError());
   // Fallback: copy + plain onesweep, all gated on the flag word.
-  cond_copy_kernel<<<context_launch(ctx, stream).num_sms * 8, 256, 0, s>>>(keys, vals, keys_out, vals_out, n, d_flags);
-  Launch L = context_launch(ctx, stream);
+  cond_copy_kernel<<<L0.num_sms * 8, 256, 0, s>>>(keys, vals, keys_out, vals_out, n, d_flags);
+  Launch L = L0;
   L.run_if = d_flags;
   const SortWorkspace SW = carve_sort_workspace(W.sort_ws, n, 8, 0);
   LTRY(ctx, cudaMemsetAsync(SW.header, 0, SW.header_words * 4, s));

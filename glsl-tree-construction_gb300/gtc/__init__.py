@@ -458,7 +458,7 @@ def build_octree_batched(ctx: Context, pts, offsets, min_coord=0.0, rng=1024.0) 
 
 
 OP_LEARNED_SORT = 6
-LEARNED_FLAGS = {1: "overflow", 2: "order", 4: "non-monotone model", 8: "long run of equal keys"}
+LEARNED_FLAGS = {1: "overflow", 2: "order", 4: "non-monotone model"}
 
 
 class LearnedModel:

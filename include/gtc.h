@@ -316,13 +316,14 @@ GTC_API gtc_status gtc_sort_pairs_u32_noalloc(gtc_ctx* ctx, uint32_t* keys, uint
  * The model is a piecewise-linear CDF with `buckets` segments (a power of two
  * <= 8192): knots at quantiles of a sample of previously sorted keys, FP32
  * heights trained on the GPU (forward / backward / Adam kernels, mean squared
- * error against the sample's empirical CDF).  gtc_learned_sort_u64 scatters
- * the keys into `buckets` buckets in one pass, sorts each bucket on chip, and
+ * error against the sample's empirical CDF).  gtc_learned_sort_u64 groups
+ * the keys by model bucket (two stable passes over the bucket-id digits, equal
+ * keys kept in input order), sorts each bucket on chip, and
  * checks on the device that no bucket overflowed its on-chip capacity (16384
  * keys) and that bucket key ranges are ordered.  If a check fails the flag
  * word *d_flags is nonzero and the plain onesweep, launched in the same stream
  * and gated on that word, produces the result instead (bits: 1 overflow,
- * 2 order, 4 non-monotone model, 8 long run of equal keys). */
+ * 2 order, 4 non-monotone model; 8 is reserved). */
 typedef struct gtc_learned_model gtc_learned_model;
 GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learned_model** out);
 GTC_API gtc_status gtc_learned_model_destroy(gtc_learned_model* model);
