@@ -49,10 +49,27 @@ __global__ void __launch_bounds__(SCAN_THREADS) unique_kernel(const K* kin, cons
   const uint32_t valid = min((uint32_t)SCAN_TILE, n - base);
   // Every read of this tile's input (and the halo) happens before the tile
   // publishes its aggregate, and every write happens after its look-back
-  // completes, so in-place compaction (kin == kout) is safe.
-  for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
-    s.keys[i] = kin[base + i];
-    if (HAS_VALS) s.vals[i] = vin[base + i];
+  // completes, so in-place compaction (kin == kout) is safe.  A full tile
+  // issues all of a thread's loads before storing any (the look-back chain
+  // makes each tile's latency the cost, not the bandwidth).
+  if (valid == SCAN_TILE) {
+    K kr[SCAN_IPT];
+    uint32_t vr[SCAN_IPT];
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; ++j) {
+      kr[j] = kin[base + j * SCAN_THREADS + tid];
+      if (HAS_VALS) vr[j] = vin[base + j * SCAN_THREADS + tid];
+    }
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; ++j) {
+      s.keys[j * SCAN_THREADS + tid] = kr[j];
+      if (HAS_VALS) s.vals[j * SCAN_THREADS + tid] = vr[j];
+    }
+  } else {
+    for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
+      s.keys[i] = kin[base + i];
+      if (HAS_VALS) s.vals[i] = vin[base + i];
+    }
   }
   if (tid == 0) s.halo = (base > 0) ? kin[base - 1] : K(0);
   __syncthreads();
@@ -159,9 +176,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(const uint32_t* in, 
     return;
   }
   const uint32_t valid = min((uint32_t)SCAN_TILE, count - base);
-  for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
-    const uint32_t g = base + i;
-    s.vals[i] = (g < limit) ? in[g] : 0u;
+  if (valid == SCAN_TILE && base + SCAN_TILE <= limit) {  // all loads of a thread in flight at once
+    uint32_t r[SCAN_IPT];
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; ++j) r[j] = in[base + j * SCAN_THREADS + tid];
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; ++j) s.vals[j * SCAN_THREADS + tid] = r[j];
+  } else {
+    for (uint32_t i = tid; i < valid; i += SCAN_THREADS) {
+      const uint32_t g = base + i;
+      s.vals[i] = (g < limit) ? in[g] : 0u;
+    }
   }
   __syncthreads();
   uint32_t v[SCAN_IPT];

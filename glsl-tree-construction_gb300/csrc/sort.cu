@@ -142,9 +142,21 @@ __global__ void __launch_bounds__(THREADS) morton_hist_kernel(const float4* __re
   zero_region(zero_ptr, zero_words);
   __syncthreads();
   const size_t stride = (size_t)gridDim.x * THREADS;
-  for (size_t i = (size_t)blockIdx.x * THREADS + threadIdx.x; i < n; i += stride) {
-    const float4 p = __ldcs(pts + i);
-    const K k = encode_point<K>(p, mn, rg);
+  size_t i = (size_t)blockIdx.x * THREADS + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {  // four points in flight per thread
+    float4 p[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[u] = __ldcs(pts + i + u * stride);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const K k = encode_point<K>(p[u], mn, rg);
+      keys[i + u * stride] = k;
+      idx[i + u * stride] = (uint32_t)(i + u * stride);
+      hist_add<K>(s_hist, k, 0, end_bit, passes);
+    }
+  }
+  for (; i < n; i += stride) {
+    const K k = encode_point<K>(__ldcs(pts + i), mn, rg);
     keys[i] = k;
     idx[i] = (uint32_t)i;
     hist_add<K>(s_hist, k, 0, end_bit, passes);
@@ -166,8 +178,8 @@ struct OnesweepSmem {
   uint32_t tile_id;
 };
 
-template <class K, int THREADS, int KPT, bool HAS_VALS>
-__global__ void __launch_bounds__(THREADS) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t dmask,
                                                            const uint32_t* __restrict__ bin_off,
@@ -494,9 +506,12 @@ struct Variant {
   int threads;
   int kpt;
   int kind;
+  int min_blocks;  // kind 0: __launch_bounds__ minimum CTAs per SM (caps registers: an
+                   // explicit 1 lets the compiler spend ~116 registers and run slower)
 };
-constexpr Variant kVariants[] = {{256, 16, 0}, {384, 16, 0}, {512, 12, 0},
-                                 {256, 16, 1}, {256, 16, 2}, {512, 8, 2}, {256, 24, 2}};
+constexpr Variant kVariants[] = {{256, 16, 0, 3}, {384, 16, 0, 2}, {512, 12, 0, 2}, {256, 16, 1, 1},
+                                 {256, 16, 2, 1}, {512, 8, 2, 1},  {256, 24, 2, 1}, {256, 16, 0, 4},
+                                 {512, 8, 0, 2},  {384, 12, 0, 3}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
 static int g_pinned[2] = {-1, -1};  // gtc_sort_set_variant: overrides the tuned choice
@@ -508,12 +523,12 @@ int sort_select_variant(int key_bits, int bits, uint32_t n) {
   return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
 }
 
-template <class K, int THREADS, int KPT, bool HV>
+template <class K, int THREADS, int KPT, bool HV, int MINB>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
                               uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
                               uint32_t* tile_counter) {
   using S = OnesweepSmem<K, THREADS, KPT>;
-  auto kern = onesweep_kernel<K, THREADS, KPT, HV>;
+  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB>;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
@@ -556,20 +571,23 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
   // one-tile-per-CTA kernel of the same tile width.
   const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
   if (kVariants[v].kind != 0 && !aligned) v = 0;
-#define GTC_OS(T, P)                                                                                     \
-  return hv ? launch_one<K, T, P, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)   \
-            : launch_one<K, T, P, false>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_OS(T, P, MB)                                                                                     \
+  return hv ? launch_one<K, T, P, true, MB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)   \
+            : launch_one<K, T, P, false, MB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
 #define GTC_TMA(T, P, M)                                                                                     \
   return hv ? launch_tma<K, T, P, true, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)    \
             : launch_tma<K, T, P, false, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
   switch (v) {
-    case 0: GTC_OS(256, 16);
-    case 1: GTC_OS(384, 16);
-    case 2: GTC_OS(512, 12);
+    case 0: GTC_OS(256, 16, 3);
+    case 1: GTC_OS(384, 16, 2);
+    case 2: GTC_OS(512, 12, 2);
     case 3: GTC_TMA(256, 16, true);
     case 4: GTC_TMA(256, 16, false);
     case 5: GTC_TMA(512, 8, false);
-    default: GTC_TMA(256, 24, false);
+    case 6: GTC_TMA(256, 24, false);
+    case 7: GTC_OS(256, 16, 4);
+    case 8: GTC_OS(512, 8, 2);
+    default: GTC_OS(384, 12, 3);
   }
 #undef GTC_OS
 #undef GTC_TMA
@@ -624,7 +642,7 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
                                float rg, const SortWorkspace& W, int passes) {
   constexpr int T = 512;
   const uint32_t want = ceil_div(n, T * 8);
-  const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 2));
+  const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 4));  // 2048 threads per SM
   morton_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(pts, keys, idx, n, mn, rg, 3 * KeyTraits<K>::B, passes,
                                                      W.counts, W.bin_offsets, W.header, W.desc, W.desc_words);
   return cudaGetLastError();
