@@ -134,7 +134,7 @@ __device__ __forceinline__ TileRange tile_range(uint32_t t, const uint32_t* tile
 // histograms; also clears the look-back descriptors of all passes.
 __global__ void __launch_bounds__(BT_THREADS) bt_morton_kernel(const float4* __restrict__ pts, const uint32_t* off,
                                                                uint32_t S, const uint32_t* tile_start, float mn,
-                                                               float rg, uint32_t* __restrict__ keys,
+                                                               float rg, float inv_rg, uint32_t* __restrict__ keys,
                                                                uint32_t* __restrict__ idx, uint32_t* seg_hist,
                                                                uint32_t* desc, size_t desc_words) {
   __shared__ uint32_t s_hist[BPASSES * BRADIX];
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(BT_THREADS) bt_morton_kernel(const float4* __r
   const uint32_t first = off[r.cloud];
   for (uint32_t i = threadIdx.x; i < r.valid; i += BT_THREADS) {
     const uint32_t g = r.base + i;
-    const uint32_t k = encode_point<uint32_t>(__ldcs(pts + g), mn, rg);
+    const uint32_t k = encode_point<uint32_t>(__ldcs(pts + g), mn, rg, inv_rg);
     keys[g] = k;
     idx[g] = g - first;
 #pragma unroll
@@ -602,7 +602,8 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
                                        L.status);
     BCHK(cudaGetLastError());
     bt_morton_kernel<<<W.tiles_max, BT_THREADS, 0, s>>>(reinterpret_cast<const float4*>(pts), d_offsets, S,
-                                                        W.tile_start, min_coord, range, W.keys_alt, W.idx_alt,
+                                                        W.tile_start, min_coord, range, pow2_reciprocal(range),
+                                                        W.keys_alt, W.idx_alt,
                                                         W.seg_hist, W.desc, W.desc_words);
     BCHK(cudaGetLastError());
     bt_seg_scan_kernel<<<S, BRADIX, 0, s>>>(W.seg_hist, d_offsets);

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "gtc.h"
 
 namespace gtc {
@@ -58,6 +60,30 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 }
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ------------------------------------------------- L2 eviction priority --
+// Loads that tag their lines for L2 to keep (evict_last: data read again soon
+// by the same kernel) or to drop first (evict_first: last use).
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_drop_policy() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint32_t ld_hint(const uint32_t* p, uint64_t pol) {
+  uint32_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint64_t ld_hint(const uint64_t* p, uint64_t pol) {
+  uint64_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+  return v;
 }
 
 // Waits until *p carries a flag, at most SPIN_LIMIT polls.  On expiry records
@@ -153,9 +179,43 @@ __device__ __forceinline__ uint32_t f2u_sat(float a) {
 }
 
 // morton.comp:50-56: (v - min) / range, then * 2^B, each op rounded to nearest.
-__device__ __forceinline__ uint32_t quantize(float v, float mn, float rg, float scale) {
-  const float t = __fdiv_rn(__fsub_rn(v, mn), rg);
+// inv_rg != 0 is 1 / range for a range that is a power of two
+// (pow2_reciprocal): the quotient and the product by the exact reciprocal are
+// the same real number rounded once, so they are the same float, and the
+// product costs one instruction instead of a full division.  Q picks the
+// form at compile time (1: product, 2: division) or per call (0).
+template <int Q = 0>
+__device__ __forceinline__ uint32_t quantize(float v, float mn, float rg, float inv_rg, float scale) {
+  const float d = __fsub_rn(v, mn);
+  float t;
+  if (Q == 1)
+    t = __fmul_rn(d, inv_rg);
+  else if (Q == 2)
+    t = __fdiv_rn(d, rg);
+  else
+    t = (inv_rg != 0.0f) ? __fmul_rn(d, inv_rg) : __fdiv_rn(d, rg);
   return f2u_sat(__fmul_rn(t, scale));
+}
+
+// 1 / rg when rg is a power of two whose reciprocal is a normal float, else 0.
+inline float pow2_reciprocal(float rg) {
+  if (!(rg > 0.0f) || !(rg < 3.0e38f)) return 0.0f;
+  int e = 0;
+  const float m = std::frexp(rg, &e);
+  if (m != 0.5f) return 0.0f;
+  const int k = 1 - e;  // rg = 2^(e - 1)
+  if (k < -126 || k > 127) return 0.0f;
+  return std::ldexp(1.0f, k);
+}
+
+// The low 11 bits of v spread to every third bit (bit i -> bit 3i).
+__device__ __forceinline__ uint32_t spread11(uint32_t v) {
+  uint32_t x = v & 0x7ffu;
+  x = (x | x << 16) & 0xff0000ffu;
+  x = (x | x << 8) & 0x0f00f00fu;
+  x = (x | x << 4) & 0xc30c30c3u;
+  x = (x | x << 2) & 0x49249249u;
+  return x;
 }
 
 __device__ __forceinline__ uint32_t split3_32(uint32_t b) {  // morton.comp:36-44
@@ -193,18 +253,34 @@ __device__ __forceinline__ uint32_t third_bits(uint64_t m) {
   return (uint32_t)x;
 }
 
-template <class K>
-__device__ __forceinline__ K encode_point(float4 p, float mn, float rg);
-template <>
-__device__ __forceinline__ uint32_t encode_point<uint32_t>(float4 p, float mn, float rg) {
-  return split3_32(quantize(p.x, mn, rg, 1024.0f)) | (split3_32(quantize(p.y, mn, rg, 1024.0f)) << 1) |
-         (split3_32(quantize(p.z, mn, rg, 1024.0f)) << 2);
-}
-template <>
-__device__ __forceinline__ uint64_t encode_point<uint64_t>(float4 p, float mn, float rg) {
-  const float s = 2097152.0f;
-  return split3_64(quantize(p.x, mn, rg, s)) | (split3_64(quantize(p.y, mn, rg, s)) << 1) |
-         (split3_64(quantize(p.z, mn, rg, s)) << 2);
+template <class K, int Q = 0>
+struct Encoder;
+template <int Q>
+struct Encoder<uint32_t, Q> {
+  static __device__ __forceinline__ uint32_t run(float4 p, float mn, float rg, float inv_rg) {
+    return split3_32(quantize<Q>(p.x, mn, rg, inv_rg, 1024.0f)) |
+           (split3_32(quantize<Q>(p.y, mn, rg, inv_rg, 1024.0f)) << 1) |
+           (split3_32(quantize<Q>(p.z, mn, rg, inv_rg, 1024.0f)) << 2);
+  }
+};
+template <int Q>
+struct Encoder<uint64_t, Q> {
+  static __device__ __forceinline__ uint64_t run(float4 p, float mn, float rg, float inv_rg) {
+  // split3_64(x) | split3_64(y) << 1 | split3_64(z) << 2, built as two 32-bit
+  // halves: x, y bits 0..10 and z bits 0..9 fill the low word, the rest the
+  // high word.
+    const float s = 2097152.0f;
+    const uint32_t x = quantize<Q>(p.x, mn, rg, inv_rg, s) & 0x1fffffu;
+    const uint32_t y = quantize<Q>(p.y, mn, rg, inv_rg, s) & 0x1fffffu;
+    const uint32_t z = quantize<Q>(p.z, mn, rg, inv_rg, s) & 0x1fffffu;
+    const uint32_t lo = spread11(x) | (spread11(y) << 1) | (spread11(z & 0x3ffu) << 2);
+    const uint32_t hi = (spread11(x >> 11) << 1) | (spread11(y >> 11) << 2) | spread11(z >> 10);
+    return ((uint64_t)hi << 32) | lo;
+  }
+};
+template <class K, int Q = 0>
+__device__ __forceinline__ K encode_point(float4 p, float mn, float rg, float inv_rg) {
+  return Encoder<K, Q>::run(p, mn, rg, inv_rg);
 }
 
 // morton32_to_xyz (morton.rs:43-60): (q / 2^B) * range + min, no contraction.

@@ -8,10 +8,11 @@ namespace gtc {
 
 template <class K>
 __global__ void __launch_bounds__(256) morton_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
-                                                     uint32_t* __restrict__ idx, uint32_t n, float mn, float rg) {
+                                                     uint32_t* __restrict__ idx, uint32_t n, float mn, float rg,
+                                                     float inv_rg) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    keys[i] = encode_point<K>(__ldcs(pts + i), mn, rg);
+    keys[i] = encode_point<K>(__ldcs(pts + i), mn, rg, inv_rg);
     if (idx) idx[i] = (uint32_t)i;
   }
 }
@@ -21,7 +22,7 @@ static cudaError_t launch_morton(const Launch& L, const float4* pts, K* keys, ui
                                  float rg) {
   if (n == 0) return cudaSuccess;
   const uint32_t grid = max(1u, min(ceil_div(n, 256 * 4), (uint32_t)L.num_sms * 16));
-  morton_kernel<K><<<grid, 256, 0, L.stream>>>(pts, keys, idx, n, mn, rg);
+  morton_kernel<K><<<grid, 256, 0, L.stream>>>(pts, keys, idx, n, mn, rg, pow2_reciprocal(rg));
   return cudaGetLastError();
 }
 

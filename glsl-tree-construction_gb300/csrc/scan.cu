@@ -22,6 +22,255 @@ size_t scan_workspace_bytes(uint32_t n) {
   return align_up((64 + (size_t)tiles) * 4, 256);
 }
 
+// --------------------------------------------------------- segment scans --
+// Resident form of the two scans, used when the input is large enough to fill
+// the GPU: a grid of co-resident blocks (at most what the SMs hold at once),
+// each owning CS_WARPS consecutive segments of S items, one per warp.
+//   1. every warp reduces its segment (coalesced row loads, many in flight);
+//      the block posts its total as a descriptor;
+//   2. the block adds up the totals of all lower blocks (one load per thread,
+//      a single round trip: every block posts before it waits, and it waits
+//      only on lower blocks, all resident);
+//   3. every warp re-reads its segment (mostly from L2) and writes it with
+//      warp-only scans: no block barrier, no staging in shared memory.
+// The single-pass kernels above pay a chained look-back per 4.6K-item tile;
+// here each block waits once.
+constexpr int CS_THREADS = 512;
+constexpr int CS_WARPS = CS_THREADS / 32;
+
+// Exclusive prefix of this block over the descriptors of blocks [0, t), and
+// the block's own segment prefixes (s_seg: per-warp totals in, exclusive
+// prefixes out).  Publishes the block total first.  Returns the prefix.
+__device__ __forceinline__ uint32_t cs_block_prefix(uint32_t* desc, uint32_t* s_seg, uint32_t* s_red,
+                                                    uint32_t* status) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t t = blockIdx.x;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t v = (lane < CS_WARPS) ? s_seg[lane] : 0u;
+    const uint32_t inc = warp_inclusive_sum(v);
+    if (lane < CS_WARPS) s_seg[lane] = inc - v;
+    if (lane == 31) st_relaxed(desc + t, (inc << 2) | FLAG_AGGREGATE);
+  }
+  uint32_t acc = 0;
+  for (uint32_t i = tid; i < t; i += CS_THREADS) acc += spin_descriptor(desc + i, status) >> 2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) s_red[warp] = acc;
+  __syncthreads();
+  uint32_t pre = 0;
+#pragma unroll
+  for (int w = 0; w < CS_WARPS; ++w) pre += s_red[w];
+  return pre;
+}
+
+// Inclusive scan with the node-offset rules of scan_kernel.  Rows of 128
+// items (one uint4 per lane); S is a multiple of 128, so rows never straddle
+// segments and in/out must be 16-byte aligned.
+__global__ void __launch_bounds__(CS_THREADS) chunk_scan_kernel(const uint32_t* __restrict__ in,
+                                                                uint32_t* __restrict__ out, uint32_t count_host,
+                                                                const uint32_t* d_u, int node_offsets, uint32_t* ws,
+                                                                uint32_t* d_o, uint32_t* status) {
+  __shared__ uint32_t s_seg[CS_WARPS];
+  __shared__ uint32_t s_red[CS_WARPS];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t count = d_u ? *d_u : count_host;
+  const uint32_t limit = node_offsets ? (count > 0 ? count - 1 : 0) : count;
+  if (count == 0) {
+    if (node_offsets && blockIdx.x == 0 && tid == 0 && d_o) *d_o = 0;
+    return;
+  }
+  const uint32_t nseg = gridDim.x * CS_WARPS;
+  const uint64_t S = (((uint64_t)count + nseg - 1) / nseg + 127) & ~(uint64_t)127;
+  const uint64_t beg64 = (uint64_t)(blockIdx.x * CS_WARPS + warp) * S;
+  const uint32_t beg = (uint32_t)min(beg64, (uint64_t)count);
+  const uint32_t end = (uint32_t)min(beg64 + S, (uint64_t)count);
+  const uint32_t full_end = beg + ((min(end, limit) > beg ? min(end, limit) - beg : 0u) & ~127u);
+  const uint4* in4 = reinterpret_cast<const uint4*>(in);
+
+  // 1. segment totals
+  uint32_t sum = 0;
+  uint32_t r = beg;
+  for (; r + 4 * 128 <= full_end; r += 4 * 128) {
+    uint4 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = in4[(r + j * 128) / 4 + lane];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sum += v[j].x + v[j].y + v[j].z + v[j].w;
+  }
+  for (; r < full_end; r += 128) {
+    const uint4 v = in4[r / 4 + lane];
+    sum += v.x + v.y + v.z + v.w;
+  }
+  for (uint32_t i = r + lane; i < end; i += 32) sum += (i < limit) ? in[i] : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) s_seg[warp] = sum;
+
+  // 2. block prefix
+  uint32_t run = cs_block_prefix(ws + 64, s_seg, s_red, status);
+  run += s_seg[warp];
+
+  // 3. rescan and write
+  for (r = beg; r < end; r += 128) {
+    const uint32_t i0 = r + 4 * lane;
+    uint4 v;
+    if (r + 128 <= full_end) {
+      v = in4[r / 4 + lane];
+    } else {
+      v.x = (i0 + 0 < end && i0 + 0 < limit) ? in[i0 + 0] : 0u;
+      v.y = (i0 + 1 < end && i0 + 1 < limit) ? in[i0 + 1] : 0u;
+      v.z = (i0 + 2 < end && i0 + 2 < limit) ? in[i0 + 2] : 0u;
+      v.w = (i0 + 3 < end && i0 + 3 < limit) ? in[i0 + 3] : 0u;
+    }
+    v.y += v.x;
+    v.z += v.y;
+    v.w += v.z;
+    const uint32_t inc = warp_inclusive_sum(v.w);
+    const uint32_t base = run + inc - v.w;
+    v.x += base;
+    v.y += base;
+    v.z += base;
+    v.w += base;
+    run += __shfl_sync(0xffffffffu, inc, 31);
+    if (node_offsets && i0 == 0) v.x = 0;
+    if (i0 + 4 <= end) {
+      reinterpret_cast<uint4*>(out)[i0 / 4] = v;
+    } else {
+      if (i0 + 0 < end) out[i0 + 0] = v.x;
+      if (i0 + 1 < end) out[i0 + 1] = v.y;
+      if (i0 + 2 < end) out[i0 + 2] = v.z;
+    }
+    if (node_offsets && d_o && i0 <= count - 1 && count - 1 < i0 + 4) {
+      const uint32_t j = count - 1 - i0;
+      const uint32_t last = (count == 1) ? 0u : (j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w);
+      *d_o = 1 + last;
+    }
+  }
+}
+
+// Unique, out of place (kin != kout: a segment is read twice, so no output
+// may land on input not yet re-read).  Rows of 32 keys; keep = first key or
+// different from its predecessor; kept keys of a row are written contiguously.
+template <class K, bool HAS_VALS>
+__global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __restrict__ kin,
+                                                                  const uint32_t* __restrict__ vin,
+                                                                  K* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                                  uint32_t n, uint32_t* ws, uint32_t* d_count,
+                                                                  uint32_t* status) {
+  __shared__ uint32_t s_seg[CS_WARPS];
+  __shared__ uint32_t s_red[CS_WARPS];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t nseg = gridDim.x * CS_WARPS;
+  const uint64_t S = (((uint64_t)n + nseg - 1) / nseg + 31) & ~(uint64_t)31;
+  const uint64_t beg64 = (uint64_t)(blockIdx.x * CS_WARPS + warp) * S;
+  const uint32_t beg = (uint32_t)min(beg64, (uint64_t)n);
+  const uint32_t end = (uint32_t)min(beg64 + S, (uint64_t)n);
+  const uint32_t full_end = beg + ((end - beg) & ~127u);
+  const K first_prev = (beg > 0 && beg < end) ? kin[beg - 1] : K(0);
+
+  // 1. kept keys per segment (keys tagged to stay in L2 for step 3)
+  const uint64_t keep_pol = l2_keep_policy(), drop_pol = l2_drop_policy();
+  uint32_t cnt = 0;
+  {
+    K carry = first_prev;
+    uint32_t r = beg;
+    for (; r < full_end; r += 128) {
+      K k[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) k[j] = ld_hint(kin + r + 32 * j + lane, keep_pol);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        K prev = __shfl_up_sync(0xffffffffu, k[j], 1);
+        if (lane == 0) prev = carry;
+        const bool keep = (r + 32 * j + lane == 0) || k[j] != prev;
+        cnt += __popc(__ballot_sync(0xffffffffu, keep));
+        carry = __shfl_sync(0xffffffffu, k[j], 31);
+      }
+    }
+    for (; r < end; r += 32) {
+      const uint32_t i = r + lane;
+      const K key = (i < end) ? kin[i] : K(0);
+      K prev = __shfl_up_sync(0xffffffffu, key, 1);
+      if (lane == 0) prev = carry;
+      const bool keep = i < end && (i == 0 || key != prev);
+      cnt += __popc(__ballot_sync(0xffffffffu, keep));
+      carry = __shfl_sync(0xffffffffu, key, 31);
+    }
+  }
+  if (lane == 0) s_seg[warp] = cnt;
+
+  // 2. block prefix
+  const uint32_t pre = cs_block_prefix(ws + 64, s_seg, s_red, status);
+  uint32_t run = pre + s_seg[warp];
+
+  // 3. rescan and write
+  {
+    K carry = first_prev;
+    uint32_t r = beg;
+    for (; r < full_end; r += 128) {
+      K k[4];
+      uint32_t v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        k[j] = ld_hint(kin + r + 32 * j + lane, drop_pol);
+        if (HAS_VALS) v[j] = ld_hint(vin + r + 32 * j + lane, drop_pol);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        K prev = __shfl_up_sync(0xffffffffu, k[j], 1);
+        if (lane == 0) prev = carry;
+        const bool keep = (r + 32 * j + lane == 0) || k[j] != prev;
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const uint32_t o = run + __popc(bal & lt);
+          kout[o] = k[j];
+          if (HAS_VALS) vout[o] = v[j];
+        }
+        run += __popc(bal);
+        carry = __shfl_sync(0xffffffffu, k[j], 31);
+      }
+    }
+    for (; r < end; r += 32) {
+      const uint32_t i = r + lane;
+      const K key = (i < end) ? kin[i] : K(0);
+      const uint32_t val = (HAS_VALS && i < end) ? vin[i] : 0u;
+      K prev = __shfl_up_sync(0xffffffffu, key, 1);
+      if (lane == 0) prev = carry;
+      const bool keep = i < end && (i == 0 || key != prev);
+      const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const uint32_t o = run + __popc(bal & lt);
+        kout[o] = key;
+        if (HAS_VALS) vout[o] = val;
+      }
+      run += __popc(bal);
+      carry = __shfl_sync(0xffffffffu, key, 31);
+    }
+  }
+  // The last warp of the last block ends at n: its running count is u.
+  if (d_count && blockIdx.x == gridDim.x - 1 && warp == CS_WARPS - 1 && lane == 0) *d_count = run;
+}
+
+// Blocks of a resident grid for the segment scans (0: use the single-pass
+// kernels).  Capped by the descriptor words of the workspace.
+// `resident` caches the kernel's resident block count (~0u: not yet known).
+static uint32_t chunk_grid(const Launch& L, const void* kern, uint32_t n_max, uint32_t* resident) {
+  if (*resident == ~0u) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, CS_THREADS, 0) != cudaSuccess || occ <= 0) {
+      cudaGetLastError();
+      occ = 0;
+    }
+    *resident = (uint32_t)occ * (uint32_t)L.num_sms;
+  }
+  const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);  // descriptor words cleared by the launcher
+  const uint32_t g = min(*resident, tiles);
+  // Worth it once every warp has a few rows to stream.
+  return (g >= 64 && (uint64_t)n_max >= (uint64_t)g * CS_WARPS * 256) ? g : 0u;
+}
+
 // ---------------------------------------------------------------- unique --
 template <class K>
 struct UniqueSmem {
@@ -122,6 +371,20 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
   cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
   if (e != cudaSuccess) return e;
   if (n == 0) return d_count ? cudaMemsetAsync(d_count, 0, 4, L.stream) : cudaSuccess;
+  if (kin != kout && vin != vout) {
+    static uint32_t grid[2] = {~0u, ~0u};  // per instantiation, for n_max = n (queried once, before any capture)
+    const int hv = vin ? 1 : 0;
+    const void* kern = vin ? (const void*)chunk_unique_kernel<K, true> : (const void*)chunk_unique_kernel<K, false>;
+    const uint32_t g = chunk_grid(L, kern, n, &grid[hv]);
+    if (g) {
+      if (vin)
+        chunk_unique_kernel<K, true><<<g, CS_THREADS, 0, L.stream>>>(kin, vin, kout, vout, n, w, d_count, L.status);
+      else
+        chunk_unique_kernel<K, false><<<g, CS_THREADS, 0, L.stream>>>(kin, nullptr, kout, nullptr, n, w, d_count,
+                                                                       L.status);
+      return cudaGetLastError();
+    }
+  }
   const size_t smem = sizeof(UniqueSmem<K>);
   static bool attr_set[2] = {false, false};  // per instantiation: set once, outside any graph capture
   if (vin) {
@@ -227,7 +490,13 @@ static cudaError_t launch_scan(const Launch& L, const uint32_t* in, uint32_t* ou
   const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);
   cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
   if (e != cudaSuccess) return e;
-  scan_kernel<<<tiles, SCAN_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
+  static uint32_t grid = ~0u;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
+  const uint32_t g = aligned ? chunk_grid(L, (const void*)chunk_scan_kernel, n_max, &grid) : 0u;
+  if (g)
+    chunk_scan_kernel<<<g, CS_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
+  else
+    scan_kernel<<<tiles, SCAN_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
   return cudaGetLastError();
 }
 

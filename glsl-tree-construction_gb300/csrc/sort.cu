@@ -129,10 +129,11 @@ __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restric
 
 // Fused Morton encode + iota payload + global histogram: the first stage of
 // the pipeline reads the points once and leaves the sort ready to run.
-template <class K, int THREADS>
-__global__ void __launch_bounds__(THREADS) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
+template <class K, int THREADS, int Q>
+__global__ void __launch_bounds__(THREADS, 2) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
                                                               uint32_t* __restrict__ idx, uint32_t n, float mn,
-                                                              float rg, int end_bit, int passes, uint32_t* counts,
+                                                              float rg, float inv_rg, int end_bit, int passes,
+                                                              uint32_t* counts,
                                                               uint32_t* bin_offsets, uint32_t* done,
                                                               uint32_t* zero_ptr, size_t zero_words) {
   __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
@@ -149,14 +150,14 @@ __global__ void __launch_bounds__(THREADS) morton_hist_kernel(const float4* __re
     for (int u = 0; u < 4; ++u) p[u] = __ldcs(pts + i + u * stride);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const K k = encode_point<K>(p[u], mn, rg);
+      const K k = encode_point<K, Q>(p[u], mn, rg, inv_rg);
       keys[i + u * stride] = k;
       idx[i + u * stride] = (uint32_t)(i + u * stride);
       hist_add<K>(s_hist, k, 0, end_bit, passes);
     }
   }
   for (; i < n; i += stride) {
-    const K k = encode_point<K>(__ldcs(pts + i), mn, rg);
+    const K k = encode_point<K, Q>(__ldcs(pts + i), mn, rg, inv_rg);
     keys[i] = k;
     idx[i] = (uint32_t)i;
     hist_add<K>(s_hist, k, 0, end_bit, passes);
@@ -641,10 +642,21 @@ template <class K>
 cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t* idx, uint32_t n, float mn,
                                float rg, const SortWorkspace& W, int passes) {
   constexpr int T = 512;
+  const float inv = pow2_reciprocal(rg);
+  auto kern = (inv != 0.0f) ? morton_hist_kernel<K, T, 1> : morton_hist_kernel<K, T, 2>;
+  // One resident wave: every block loops over the points.
+  static int resident[2] = {0, 0};  // blocks per SM of each form, queried once
+  int& occ = resident[inv != 0.0f ? 0 : 1];
+  if (occ == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, T, 0) != cudaSuccess || occ < 1) {
+      cudaGetLastError();
+      occ = 2;
+    }
+  }
   const uint32_t want = ceil_div(n, T * 8);
-  const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 4));  // 2048 threads per SM
-  morton_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(pts, keys, idx, n, mn, rg, 3 * KeyTraits<K>::B, passes,
-                                                     W.counts, W.bin_offsets, W.header, W.desc, W.desc_words);
+  const uint32_t grid = max(1u, min(want, (uint32_t)(L.num_sms * occ)));
+  kern<<<grid, T, 0, L.stream>>>(pts, keys, idx, n, mn, rg, inv, 3 * KeyTraits<K>::B, passes, W.counts,
+                                 W.bin_offsets, W.header, W.desc, W.desc_words);
   return cudaGetLastError();
 }
 template cudaError_t launch_morton_hist<uint32_t>(const Launch&, const float4*, uint32_t*, uint32_t*, uint32_t, float,

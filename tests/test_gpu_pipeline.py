@@ -46,6 +46,15 @@ def test_config2_clustered_10m(ctx, oracle):
 
 
 @pytest.mark.parametrize("key_bits", [32, 64])
+def test_many_duplicates_3m(ctx, oracle, key_bits):
+    """3M points in a few tight clusters: most Morton codes repeat, so unique
+    compacts heavily (its resident segment form runs at this size), and the
+    node-offset scan sees long runs of nodes."""
+    pts = W.gaussian_mixture_points(3_000_000, 4, 1.5, noise=0.01, seed=23)
+    _run(ctx, oracle, pts, key_bits, "dups")
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
 def test_edge_cases(ctx, oracle, key_bits):
     def p(xyz):
         xyz = np.asarray(xyz, np.float32).reshape(-1, 3)

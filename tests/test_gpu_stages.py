@@ -53,6 +53,22 @@ def test_morton_boundary_values(ctx, oracle):
 
 
 @pytest.mark.parametrize("key_bits", [32, 64])
+def test_morton_ranges(ctx, oracle, key_bits):
+    """Power-of-two ranges take the exact-reciprocal product, others the
+    division; both must give the reference's quantisation bit for bit,
+    including tiny differences that round into subnormals."""
+    rng = np.random.default_rng(5)
+    kd = np.uint32 if key_bits == 32 else np.uint64
+    for mn, rg in ((0.0, 1024.0), (-3.5, 1000.0), (10.0, 2.0 ** -20), (-1e-30, 2.0 ** 100), (0.25, 3.0),
+                   (0.0, 2.0 ** 126), (1e-38, 2.0 ** -100)):
+        pts = np.ones((50_000, 4), np.float32)
+        pts[:, :3] = (mn + rng.random((50_000, 3)) * rg * 1.1 - rg * 0.05).astype(np.float32)
+        pts[:8, :3] = np.float32(mn) + np.float32(1e-45) * np.arange(24, dtype=np.float32).reshape(8, 3)
+        keys, _ = ctx.morton(dev(pts), key_bits, mn, rg)
+        assert np.array_equal(host(keys, kd), oracle.morton(pts, key_bits, mn, rg)), (mn, rg)
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
 def test_global_histogram(ctx, oracle, key_bits):
     keys = W.config3_keys(1_000_003, key_bits, and_words=2, seed=4)
     hist = ctx.global_histogram(dev(keys), 0, key_bits)
@@ -198,7 +214,7 @@ def test_radix_tree_last_key_outlier(ctx, oracle):
     assert np.array_equal(host(t["parent"], np.int32), e["parent"])
 
 
-@pytest.mark.parametrize("n", [1, 2, 4607, 4608, 4609, 1_000_000])
+@pytest.mark.parametrize("n", [1, 2, 4607, 4608, 4609, 1_000_000, 3_000_001, 9_999_994])
 def test_partial_sum_and_node_offsets(ctx, oracle, n):
     rng = np.random.default_rng(n)
     data = rng.integers(0, 5, size=n).astype(np.uint32)
