@@ -1,6 +1,7 @@
 // api.cu - the C ABI (include/gtc.h): context, workspace, stage operators,
 // the fused stream-ordered pipeline and its host-buffer form.
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -14,6 +15,9 @@ int sort_num_variants();
 int sort_get_variant(int key_bits);
 bool sort_set_variant(int key_bits, int v);
 void sort_variant_shape(int v, int* threads, int* kpt);
+
+static std::atomic<uint32_t> g_literal{0};
+uint32_t literal_flags() { return g_literal.load(std::memory_order_relaxed); }
 }  // namespace gtc
 
 using namespace gtc;
@@ -578,7 +582,9 @@ GTC_API gtc_status gtc_edge_count(gtc_ctx* ctx, const uint8_t* prefix_n, const i
   GTC_ARG(ctx, key_bits == 32 || key_bits == 64, "key_bits must be 32 or 64");
   GTC_ARG(ctx, m == 0 || (prefix_n && parent && edge), "null buffer");
   StageTimer t(ctx, s, GTC_STAGE_RADIX_TREE);
-  GTC_TRY(ctx, launch_edge_count(launch_of(ctx, s), prefix_n, parent, edge, m, key_bits == 32 ? 2 : 1));
+  // GTC_LITERAL_D2: the reference's depth prefix_n / 3, unused bits included.
+  const int A = (literal_flags() & GTC_LITERAL_D2) ? 0 : (key_bits == 32 ? 2 : 1);
+  GTC_TRY(ctx, launch_edge_count(launch_of(ctx, s), prefix_n, parent, edge, m, A));
   return GTC_OK;
 }
 
@@ -724,5 +730,47 @@ GTC_API gtc_status gtc_sort_set_variant(int key_bits, int v) {
 GTC_API int gtc_sort_get_variant(int key_bits) { return sort_get_variant(key_bits); }
 GTC_API gtc_status gtc_tree_set_method(int method) { return tree_set_method(method) ? GTC_OK : GTC_ERR_INVALID_ARG; }
 GTC_API int gtc_tree_get_method(void) { return tree_get_method(); }
+
+GTC_API gtc_status gtc_set_literal(uint32_t flags) {
+  if (flags & ~(GTC_LITERAL_D2 | GTC_LITERAL_D6)) return GTC_ERR_INVALID_ARG;
+  g_literal.store(flags);
+  return GTC_OK;
+}
+GTC_API uint32_t gtc_get_literal(void) { return g_literal.load(); }
+
+GTC_API gtc_status gtc_gather_points(gtc_ctx* ctx, const float* pts, uint32_t n_pts, const uint32_t* idx,
+                                     uint32_t count, float* out, gtc_stream_t s) {
+  GTC_ARG(ctx, ctx, "null context");
+  if (count == 0) return GTC_OK;
+  GTC_ARG(ctx, pts && idx && out, "null buffer");
+  GTC_ARG(ctx, ((reinterpret_cast<uintptr_t>(pts) | reinterpret_cast<uintptr_t>(out)) & 15) == 0,
+          "points must be 16-byte aligned float4");
+  GTC_TRY(ctx, launch_gather_points(launch_of(ctx, s), reinterpret_cast<const float4*>(pts), n_pts, idx, count,
+                                    reinterpret_cast<float4*>(out)));
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_export_le(const char* path, const void* host_data, size_t count, int elem_bytes, int append) {
+  if (!path || (count > 0 && !host_data) || !(elem_bytes == 1 || elem_bytes == 2 || elem_bytes == 4 || elem_bytes == 8))
+    return GTC_ERR_INVALID_ARG;
+  FILE* f = std::fopen(path, append ? "ab" : "wb");
+  if (!f) return GTC_ERR_INVALID_ARG;
+  // Bytes of each element least significant first, whatever the host order.
+  const unsigned char* src = static_cast<const unsigned char*>(host_data);
+  const uint16_t probe = 1;
+  const bool little = *reinterpret_cast<const unsigned char*>(&probe) == 1;
+  bool ok = true;
+  if (little) {
+    ok = std::fwrite(src, (size_t)elem_bytes, count, f) == count;
+  } else {
+    unsigned char buf[8];
+    for (size_t i = 0; i < count && ok; ++i) {
+      for (int b = 0; b < elem_bytes; ++b) buf[b] = src[i * elem_bytes + (elem_bytes - 1 - b)];
+      ok = std::fwrite(buf, (size_t)elem_bytes, 1, f) == 1;
+    }
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? GTC_OK : GTC_ERR_INVALID_ARG;
+}
 
 }  // extern "C"

@@ -435,7 +435,8 @@ __global__ void bt_cloud_offsets_kernel(uint32_t* uoff, const uint32_t* ne_start
 __device__ __forceinline__ void bt_octree_one(uint32_t g, uint4 ci, const uint32_t* codes, const uint8_t* prefix_n,
                                               const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
                                               const uint32_t* edge, const uint32_t* ps, float mn, float rg,
-                                              gtc_octnode* nodes, uint32_t capacity, uint32_t* status) {
+                                              gtc_octnode* nodes, uint32_t capacity, uint32_t lmask_keep,
+                                              uint32_t* status) {
   constexpr int A = KeyTraits<uint32_t>::A;
   const uint32_t U0 = ci.x, k = g - U0, m = ci.y - U0 - 1, bias = ci.z, O = ci.w;
   if (O >= capacity) {
@@ -448,7 +449,7 @@ __device__ __forceinline__ void bt_octree_one(uint32_t g, uint4 ci, const uint32
   }
   const int root_level = (prefix_n[U0] - A) / 3;
   octree_make_node<uint32_t, true>(k, codes + U0, prefix_n + U0, hll + U0, hlr + U0, left + U0, edge + U0, ps + U0,
-                                   bias, root_level, mn, rg, nodes + O, capacity - O, status);
+                                   bias, root_level, mn, rg, nodes + O, capacity - O, lmask_keep, status);
 }
 
 // Octree of every cloud, and the cloud-local node offsets (what the
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restri
                                                         const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
                                                         const uint32_t* edge, const uint32_t* ps,
                                                         uint32_t* node_offsets, float mn, float rg, gtc_octnode* nodes,
-                                                        uint32_t capacity, uint32_t* status) {
+                                                        uint32_t capacity, uint32_t lmask_keep, uint32_t* status) {
   constexpr int WARPS = 256 / 32;
   __shared__ uint2 s_queue[WARPS][64];
   const uint32_t U = uoff[S];
@@ -487,7 +488,8 @@ __global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restri
     __syncwarp();
     if (qn >= 32) {
       const uint2 e = q[lane];
-      bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, status);
+      bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, lmask_keep,
+                    status);
       const uint2 rest = (lane + 32 < qn) ? q[lane + 32] : make_uint2(0, 0);
       __syncwarp();
       if (lane + 32 < qn) q[lane] = rest;
@@ -497,7 +499,8 @@ __global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restri
   }
   if (lane < qn) {
     const uint2 e = q[lane];
-    bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, status);
+    bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, lmask_keep,
+                    status);
   }
 }
 
@@ -669,7 +672,7 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
     bt_octree_kernel<<<ogrid, 256, 0, s>>>(out->keys, out->key_offset, S, reinterpret_cast<const uint4*>(W.seg_hist),
                                            out->prefix_n, out->has_leaf_left, out->has_leaf_right, out->left_child,
                                            out->edge_count, W.ps, out->node_offsets, min_coord, range, out->nodes,
-                                           out->nodes_capacity, L.status);
+                                           out->nodes_capacity, leaf_mask_keep(), L.status);
     BCHK(cudaGetLastError());
   }
 #undef BCHK

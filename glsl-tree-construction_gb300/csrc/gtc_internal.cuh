@@ -86,6 +86,9 @@ __device__ __forceinline__ uint64_t ld_hint(const uint64_t* p, uint64_t pol) {
   return v;
 }
 
+// Hint: fetch the 128-byte line holding p into L2.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Waits until *p carries a flag, at most SPIN_LIMIT polls.  On expiry records
 // DEV_TIMEOUT and returns an INCLUSIVE descriptor of value 0 so the caller's
 // look-back ends.
@@ -334,6 +337,11 @@ __device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v) {
   return v;
 }
 
+// Literal-mode switches (GTC_LITERAL_*), process-wide.
+uint32_t literal_flags();
+// child_leaf_mask bits kept by the octree kernels: none under GTC_LITERAL_D6.
+inline uint32_t leaf_mask_keep() { return (literal_flags() & GTC_LITERAL_D6) ? 0u : 0xffu; }
+
 // ------------------------------------------------------- launcher table ---
 struct Launch {
   cudaStream_t stream;
@@ -414,6 +422,8 @@ cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d
 // Radix tree method: 1 split-indexed window kernel (default), 0 per-node Karras.
 int tree_get_method();
 bool tree_set_method(int m);
+cudaError_t launch_gather_points(const Launch& L, const float4* pts, uint32_t n_pts, const uint32_t* idx,
+                                 uint32_t count, float4* out);
 cudaError_t launch_edge_count(const Launch& L, const uint8_t* prefix_n, const int32_t* parent, uint32_t* edge,
                               uint32_t m, int unused_bits);
 template <class K>

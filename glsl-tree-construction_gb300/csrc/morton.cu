@@ -26,6 +26,31 @@ static cudaError_t launch_morton(const Launch& L, const float4* pts, K* keys, ui
   return cudaGetLastError();
 }
 
+// Points in the order of a payload: out[i] = pts[idx[i]].  One 16-byte load
+// and store per point; out-of-range indices give zeros and flag the status.
+__global__ void __launch_bounds__(256) gather_points_kernel(const float4* __restrict__ pts, uint32_t n_pts,
+                                                            const uint32_t* __restrict__ idx, uint32_t count,
+                                                            float4* __restrict__ out, uint32_t* status) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint32_t j = idx[i];
+    if (j < n_pts) {
+      out[i] = pts[j];
+    } else {
+      out[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      atomicOr(status, DEV_BAD_INPUT);
+    }
+  }
+}
+
+cudaError_t launch_gather_points(const Launch& L, const float4* pts, uint32_t n_pts, const uint32_t* idx,
+                                 uint32_t count, float4* out) {
+  if (count == 0) return cudaSuccess;
+  const uint32_t grid = max(1u, min(ceil_div(count, 256 * 4), (uint32_t)L.num_sms * 16));
+  gather_points_kernel<<<grid, 256, 0, L.stream>>>(pts, n_pts, idx, count, out, L.status);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_morton32(const Launch& L, const float4* pts, uint32_t* keys, uint32_t* idx, uint32_t n, float mn,
                             float rg) {
   return launch_morton<uint32_t>(L, pts, keys, idx, n, mn, rg);

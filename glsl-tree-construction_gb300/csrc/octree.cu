@@ -45,7 +45,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
                                                   const int32_t* __restrict__ left, const uint32_t* __restrict__ edge,
                                                   const uint32_t* __restrict__ ps, uint32_t ps_bias, int root_level,
                                                   float mn, float rg, gtc_octnode* __restrict__ nodes,
-                                                  uint32_t capacity, uint32_t* status) {
+                                                  uint32_t capacity, uint32_t lmask_keep, uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
@@ -185,7 +185,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
     const int4 a = chl[0], b = chl[1];
     const uint32_t mk = S.mk[lane];
     nmask |= mk & 0xffu;
-    lmask |= mk >> 8;
+    lmask = (lmask | (mk >> 8)) & lmask_keep;
     const uint32_t bottom = (k == 0) ? 0u : top - c + 1;
     // Corners from the cell coordinates decoded once; cell sizes rg / 2^k as
     // the exact scaling rg * 2^-k (octree.comp:111-116, 181-182).
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
                                                                   const uint32_t* __restrict__ edge,
                                                                   const uint32_t* __restrict__ ps, float mn, float rg,
                                                                   gtc_octnode* __restrict__ nodes, uint32_t capacity,
-                                                                  uint32_t* status) {
+                                                                  uint32_t lmask_keep, uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
   constexpr int WARPS = OCT_THREADS / 32;
   __shared__ OctWarp s_warp[WARPS];
@@ -251,13 +251,13 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
       if (lane + 32 < qn) S.q[lane] = rest;
       qn -= 32;
       octree_warp_batch<K, WITH_LEAVES>(S, true, kk, m, codes, prefix_n, hll, hlr, left, edge, ps, 0u, root_level,
-                                        mn, rg, nodes, capacity, status);
+                                        mn, rg, nodes, capacity, lmask_keep, status);
     }
   }
   if (qn > 0) {
     const uint32_t kk = S.q[lane];
     octree_warp_batch<K, WITH_LEAVES>(S, lane < qn, kk, m, codes, prefix_n, hll, hlr, left, edge, ps, 0u, root_level,
-                                      mn, rg, nodes, capacity, status);
+                                      mn, rg, nodes, capacity, lmask_keep, status);
   }
 }
 
@@ -273,10 +273,12 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
   const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 5));
   if (with_leaves)
     octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
-                                                                     edge, ps, mn, rg, nodes, capacity, L.status);
+                                                                     edge, ps, mn, rg, nodes, capacity,
+                                                                     leaf_mask_keep(), L.status);
   else
     octree_make_kernel<K, false><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
-                                                                      edge, ps, mn, rg, nodes, capacity, L.status);
+                                                                      edge, ps, mn, rg, nodes, capacity, 0xffu,
+                                                                      L.status);
   return cudaGetLastError();
 }
 template cudaError_t launch_octree_make<uint32_t>(const Launch&, const uint32_t*, const uint32_t*, uint32_t, uint32_t,
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(256) octree_link_kernel(const K* __restrict__ 
                                                           const int32_t* __restrict__ parent,
                                                           const uint32_t* __restrict__ edge,
                                                           const uint32_t* __restrict__ ps, gtc_octnode* nodes,
-                                                          uint32_t capacity, uint32_t* status) {
+                                                          uint32_t capacity, bool leaf_mask, uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(256) octree_link_kernel(const K* __restrict__ 
       const int32_t leaf = left[i] + side;
       const int w = child_slot<K>(codes[leaf], level);
       nodes[slot].children[w] = leaf;
-      atomicOr(&nodes[slot].child_leaf_mask, 1 << w);
+      if (leaf_mask) atomicOr(&nodes[slot].child_leaf_mask, 1 << w);
     }
   }
 }
@@ -339,7 +341,7 @@ cudaError_t launch_octree_link(const Launch& L, const K* codes, uint32_t m, cons
   if (m == 0) return cudaSuccess;
   const uint32_t grid = max(1u, min(ceil_div(m, 256), (uint32_t)L.num_sms * 8));
   octree_link_kernel<K><<<grid, 256, 0, L.stream>>>(codes, m, prefix_n, hll, hlr, left, parent, edge, ps, nodes,
-                                                    capacity, L.status);
+                                                    capacity, leaf_mask_keep() != 0, L.status);
   return cudaGetLastError();
 }
 template cudaError_t launch_octree_link<uint32_t>(const Launch&, const uint32_t*, uint32_t, const uint8_t*,

@@ -120,7 +120,7 @@ __device__ __forceinline__ void octree_make_node(uint32_t k, const K* __restrict
                                                  const uint32_t* __restrict__ edge,
                                                  const uint32_t* __restrict__ ps, uint32_t ps_bias, int root_level,
                                                  float mn, float rg, gtc_octnode* __restrict__ nodes,
-                                                 uint32_t capacity, uint32_t* status) {
+                                                 uint32_t capacity, uint32_t lmask_keep, uint32_t* status) {
   constexpr int A = KeyTraits<K>::A;
   const uint32_t c = edge[k];
   if (!(k == 0 || c > 0)) return;
@@ -143,7 +143,7 @@ __device__ __forceinline__ void octree_make_node(uint32_t k, const K* __restrict
   // the exact scaling rg * 2^-k (octree.comp:111-116, 181-182).
   const uint3 q = code_xyz<K>(code_k);
   store_node(nodes, bottom, lo, hi, corner_at<K>(q, dk, mn, rg), __fmul_rn(rg, exp2_neg(dk - root_level)), nmask,
-             lmask);
+             lmask & (int32_t)lmask_keep);
   // Chain nodes above the bottom (levels dk - 1 .. dk - c + 1).
   for (uint32_t j = 1; j < c; ++j) {
     const int level = dk - (int)j;

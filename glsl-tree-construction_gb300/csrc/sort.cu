@@ -179,7 +179,7 @@ struct OnesweepSmem {
   uint32_t tile_id;
 };
 
-template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB>
+template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB, int LBW, bool EARLY>
 __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t dmask,
@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   constexpr int WARPS = S::WARPS;
   constexpr int TILE = S::TILE;
   static_assert(THREADS >= RADIX, "one thread per digit");
+  static_assert(TILE <= 65536, "warp ranks are packed in 16 bits");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S& s = *reinterpret_cast<S*>(smem_raw);
   const int tid = threadIdx.x;
@@ -201,6 +202,16 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
 
   for (int i = tid; i < WARPS * RADIX; i += THREADS) (&s.warp_hist[0][0])[i] = 0;
   if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
+  // Blocks start in about index order, so the ticket is usually close to
+  // this block's index: warm L2 with that tile while the ticket is in flight
+  // (a hint only; the tile actually processed is the ticket's).
+  {
+    const uint32_t guess = blockIdx.x * TILE;
+    constexpr uint32_t KL = 128 / sizeof(K), VL = 32;  // elements per 128-byte line
+    for (uint32_t e = guess + tid * KL; e < guess + TILE && e < n; e += THREADS * KL) prefetch_l2(kin + e);
+    if (HAS_VALS)
+      for (uint32_t e = guess + tid * VL; e < guess + TILE && e < n; e += THREADS * VL) prefetch_l2(vin + e);
+  }
   __syncthreads();
   const uint32_t tile = s.tile_id;
   const uint32_t tile_base = tile * TILE;
@@ -216,24 +227,48 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
     if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
   }
 
-  // 3. early per-warp digit counts: one shared atomic per key (one per warp
-  // when all 32 lanes share the digit, the low-entropy case).
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* my_hist = s.warp_hist[warp];
+  uint32_t rank[KPT];  // !EARLY: rank within the warp's digit run | digit << 16
+  if (EARLY) {
+    // 3. early per-warp digit counts: one shared atomic per key (one per warp
+    // when all 32 lanes share the digit, the low-entropy case).
 #pragma unroll
-  for (int j = 0; j < KPT; ++j) {
-    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-    const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-    if (__all_sync(0xffffffffu, d == d0)) {
-      if (lane == 0) atomicAdd(&my_hist[d], 32u);
-    } else {
-      atomicAdd(&my_hist[d], 1u);
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+      if (__all_sync(0xffffffffu, d == d0)) {
+        if (lane == 0) atomicAdd(&my_hist[d], 32u);
+      } else {
+        atomicAdd(&my_hist[d], 1u);
+      }
+    }
+  } else {
+    // 3'. counts and warp ranks in one sweep: the peer group's leader adds the
+    // group's size to the warp's digit counter and gets the group's base back.
+    // The scatter waits until the warp offsets are known, so the counter
+    // atomics of consecutive keys follow each other without stores between.
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      uint32_t peers = 0xffffffffu;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const uint32_t bit = (d >> b) & 1u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? bal : ~bal;
+      }
+      const int leader = 31 - __clz(peers);
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      rank[j] = (base + __popc(peers & lt_mask)) | (d << 16);
     }
   }
   __syncthreads();
 
-  // 4. per-digit counts across warps; publish the tile aggregate early; turn
-  // the per-warp counts into tile-local start positions.
+  // 4. per-digit counts across warps; publish the tile aggregate; turn the
+  // per-warp counts into tile-local start positions.
   uint32_t count = 0;
   if (tid < RADIX) {
 #pragma unroll
@@ -252,33 +287,43 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   }
   __syncthreads();
 
-  // 5. stable ranks by warp multisplit (8 __ballot_sync give the peer mask;
-  // the highest peer advances the warp's digit cursor and broadcasts the old
-  // value) and the scatter into tile-local digit order.
+  if (EARLY) {
+    // 5. stable ranks by warp multisplit (8 __ballot_sync give the peer mask;
+    // the highest peer advances the warp's digit cursor and broadcasts the old
+    // value) and the scatter into tile-local digit order.
 #pragma unroll
-  for (int j = 0; j < KPT; ++j) {
-    const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-    uint32_t peers = 0xffffffffu;
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      uint32_t peers = 0xffffffffu;
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const uint32_t bit = (d >> b) & 1u;
-      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-      peers &= bit ? bal : ~bal;
+      for (int b = 0; b < 8; ++b) {
+        const uint32_t bit = (d >> b) & 1u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? bal : ~bal;
+      }
+      const int leader = 31 - __clz(peers);
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      const uint32_t local = base + __popc(peers & lt_mask);
+      s.keys[local] = key[j];
+      if (HAS_VALS) s.vals[local] = val[j];
     }
-    const int leader = 31 - __clz(peers);
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    const uint32_t local = base + __popc(peers & lt_mask);
-    s.keys[local] = key[j];
-    if (HAS_VALS) s.vals[local] = val[j];
+  } else {
+    // 5'. scatter into tile-local digit order.
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const uint32_t local = my_hist[rank[j] >> 16] + (rank[j] & 0xffffu);
+      s.keys[local] = key[j];
+      if (HAS_VALS) s.vals[local] = val[j];
+    }
   }
 
   // 6. decoupled look-back over predecessor tiles, one thread per digit.
   if (tid < RADIX) {
     uint32_t excl = 0;
     if (tile > 0) {
-      excl = lookback_window<8, RADIX>(desc, tile, tid, status);
+      excl = lookback_window<LBW, RADIX>(desc, tile, tid, status);
       st_relaxed(desc + (size_t)tile * RADIX + tid, ((excl + count) << 2) | FLAG_INCLUSIVE);
     }
     s.global_base[tid] = bin_off[tid] + excl - digit_off;
@@ -509,10 +554,12 @@ struct Variant {
   int kind;
   int min_blocks;  // kind 0: __launch_bounds__ minimum CTAs per SM (caps registers: an
                    // explicit 1 lets the compiler spend ~116 registers and run slower)
+  int early;       // kind 0: 1 = per-key early counts, then ranks; 0 = counts and ranks in one sweep
 };
-constexpr Variant kVariants[] = {{256, 16, 0, 3}, {384, 16, 0, 2}, {512, 12, 0, 2}, {256, 16, 1, 1},
-                                 {256, 16, 2, 1}, {512, 8, 2, 1},  {256, 24, 2, 1}, {256, 16, 0, 4},
-                                 {512, 8, 0, 2},  {384, 12, 0, 3}};
+constexpr Variant kVariants[] = {{256, 16, 0, 3, 1}, {384, 16, 0, 2, 1}, {512, 12, 0, 2, 1}, {256, 16, 1, 1, 1},
+                                 {256, 16, 2, 1, 1}, {512, 8, 2, 1, 1},  {256, 24, 2, 1, 1}, {256, 16, 0, 4, 1},
+                                 {512, 8, 0, 2, 1},  {384, 12, 0, 3, 1}, {256, 16, 0, 3, 0}, {384, 16, 0, 2, 0},
+                                 {512, 12, 0, 2, 0}, {256, 24, 0, 2, 0}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
 static int g_pinned[2] = {-1, -1};  // gtc_sort_set_variant: overrides the tuned choice
@@ -524,12 +571,12 @@ int sort_select_variant(int key_bits, int bits, uint32_t n) {
   return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
 }
 
-template <class K, int THREADS, int KPT, bool HV, int MINB>
+template <class K, int THREADS, int KPT, bool HV, int MINB, bool EARLY>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
                               uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
                               uint32_t* tile_counter) {
   using S = OnesweepSmem<K, THREADS, KPT>;
-  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB>;
+  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, EARLY>;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
@@ -572,23 +619,27 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
   // one-tile-per-CTA kernel of the same tile width.
   const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
   if (kVariants[v].kind != 0 && !aligned) v = 0;
-#define GTC_OS(T, P, MB)                                                                                     \
-  return hv ? launch_one<K, T, P, true, MB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)   \
-            : launch_one<K, T, P, false, MB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_OS(T, P, MB, LB)                                                                                   \
+  return hv ? launch_one<K, T, P, true, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
+            : launch_one<K, T, P, false, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
 #define GTC_TMA(T, P, M)                                                                                     \
   return hv ? launch_tma<K, T, P, true, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)    \
             : launch_tma<K, T, P, false, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
   switch (v) {
-    case 0: GTC_OS(256, 16, 3);
-    case 1: GTC_OS(384, 16, 2);
-    case 2: GTC_OS(512, 12, 2);
+    case 0: GTC_OS(256, 16, 3, true);
+    case 1: GTC_OS(384, 16, 2, true);
+    case 2: GTC_OS(512, 12, 2, true);
     case 3: GTC_TMA(256, 16, true);
     case 4: GTC_TMA(256, 16, false);
     case 5: GTC_TMA(512, 8, false);
     case 6: GTC_TMA(256, 24, false);
-    case 7: GTC_OS(256, 16, 4);
-    case 8: GTC_OS(512, 8, 2);
-    default: GTC_OS(384, 12, 3);
+    case 7: GTC_OS(256, 16, 4, true);
+    case 8: GTC_OS(512, 8, 2, true);
+    case 9: GTC_OS(384, 12, 3, true);
+    case 10: GTC_OS(256, 16, 3, false);
+    case 11: GTC_OS(384, 16, 2, false);
+    case 12: GTC_OS(512, 12, 2, false);
+    default: GTC_OS(256, 24, 2, false);
   }
 #undef GTC_OS
 #undef GTC_TMA

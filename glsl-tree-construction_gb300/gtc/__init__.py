@@ -210,6 +210,15 @@ class Context:
         return nodes[:n_oct]
 
     # -- sort variant table (autotuner) ------------------------------------
+    def gather_points(self, pts, idx, count: int | None = None):
+        """Points in payload order: out[i] = pts[idx[i]] (float4 [count, 4])."""
+        torch = _torch()
+        count = idx.numel() if count is None else count
+        out = torch.empty((count, 4), dtype=torch.float32, device=pts.device)
+        self.check(self.L.gtc_gather_points(self.h, _ptr(pts), pts.shape[0], _ptr(idx), count, _ptr(out),
+                                            _stream()))
+        return out
+
     def sort_variants(self):
         out = []
         for v in range(self.L.gtc_sort_num_variants()):
@@ -255,6 +264,59 @@ def autotune_load(path: str):
 
 def autotune_clear():
     lib().gtc_autotune_clear()
+
+
+LITERAL_D2 = 1 << 2  # gtc_edge_count: depth = prefix_n / 3 (edge_count.comp:34)
+LITERAL_D6 = 1 << 6  # leaf links leave child_leaf_mask at 0 (octree.comp:27-30)
+
+
+def set_literal(flags: int):
+    """Process-wide literal-mode switches (LITERAL_D2 | LITERAL_D6; 0 = the
+    corrected forms)."""
+    st = lib().gtc_set_literal(flags)
+    if st != 0:
+        raise GtcError(st, f"unknown literal flags {flags:#x}")
+
+
+def get_literal() -> int:
+    return int(lib().gtc_get_literal())
+
+
+def export_le(path: str, data, append: bool = False):
+    """Write a host or device array to `path` as little-endian elements of its
+    own width (the reference's write_u32::<LittleEndian> dump)."""
+    a = data.cpu().numpy() if hasattr(data, "cpu") else np.asarray(data)
+    a = np.ascontiguousarray(a)
+    width = a.dtype.itemsize
+    st = lib().gtc_export_le(path.encode(), a.ctypes.data if a.size else None, a.size, width, int(append))
+    if st != 0:
+        raise GtcError(st, f"cannot write {path}")
+
+
+STAGE_BUFFERS = ("keys", "idx", "prefix_n", "has_leaf_left", "has_leaf_right", "left_child", "parent", "edge_count",
+                 "node_offsets", "nodes")
+
+
+def export_build(res, directory: str) -> dict:
+    """Every stage buffer of a build as `<name>.bin` (little-endian words of
+    each buffer's element width; nodes as 16 32-bit words per node), cut to
+    the live lengths (u keys and payloads, m tree entries, u node offsets, o
+    nodes).  Returns {name: path}."""
+    import os
+
+    os.makedirs(directory, exist_ok=True)
+    u, m, o = res.n_unique, res.n_brt_nodes, res.n_oct_nodes
+    live = {"keys": u, "idx": u, "prefix_n": m, "has_leaf_left": m, "has_leaf_right": m, "left_child": m,
+            "parent": m, "edge_count": m, "node_offsets": u, "nodes": o}
+    out = {}
+    for name in STAGE_BUFFERS:
+        t = getattr(res, name)
+        a = t.cpu().numpy() if hasattr(t, "cpu") else np.asarray(t)
+        a = a.reshape(-1, 16)[: live[name]] if name == "nodes" else a.reshape(-1)[: live[name]]
+        path = os.path.join(directory, name + ".bin")
+        export_le(path, a)
+        out[name] = path
+    return out
 
 
 @dataclass

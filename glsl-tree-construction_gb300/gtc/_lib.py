@@ -80,6 +80,10 @@ SIGNATURES = {
     "gtc_sort_get_variant": (i_, [i_]),
     "gtc_tree_set_method": (st, [i_]),
     "gtc_tree_get_method": (i_, []),
+    "gtc_set_literal": (st, [u32]),
+    "gtc_get_literal": (u32, []),
+    "gtc_gather_points": (st, [P, P, u32, P, u32, P, P]),
+    "gtc_export_le": (st, [ctypes.c_char_p, P, sz, i_, i_]),
     "gtc_autotune_sort": (st, [P, i_, i_, i_, u32, P, i_, ctypes.POINTER(i_), P]),
     "gtc_autotune_lookup": (i_, [i_, i_, u32]),
     "gtc_autotune_record": (st, [i_, i_, u32, i_, f32]),

@@ -396,6 +396,37 @@ GTC_API gtc_status gtc_autotune_load(const char* path);
 GTC_API gtc_status gtc_host_alloc(void** ptr, size_t bytes);
 GTC_API gtc_status gtc_host_free(void* ptr);
 
+/* Literal-mode switches, process-wide (default 0: the corrected forms).  They
+ * reproduce the reference's deterministic deviations for callers comparing
+ * against buffers the reference wrote:
+ *   GTC_LITERAL_D2  gtc_edge_count takes depth = prefix_n / 3, counting the
+ *                   unused high bits (edge_count.comp:34), instead of
+ *                   (prefix_n - A) / 3;
+ *   GTC_LITERAL_D6  leaf links leave child_leaf_mask at 0, as SetLeaf's
+ *                   `mask &= ~bit` does (octree.comp:27-30); leaf child slots
+ *                   are still written.  Applies to make, link, and the fused
+ *                   and batched builds.
+ * The literal depth is not offered for the octree itself: there it maps
+ * several children to one slot (child-slot conflicts), and the survivor
+ * depends on write order. */
+#define GTC_LITERAL_D2 (1u << 2)
+#define GTC_LITERAL_D6 (1u << 6)
+GTC_API gtc_status gtc_set_literal(uint32_t flags);
+GTC_API uint32_t gtc_get_literal(void);
+
+/* Points in sorted order: out[i] = pts[idx[i]] for i < count (float4 each),
+ * e.g. with the payload of a sort or of unique (one point per distinct
+ * code).  Indices >= n_pts give a zero point and flag GTC_ERR_INVALID_ARG on
+ * the device status word. */
+GTC_API gtc_status gtc_gather_points(gtc_ctx* ctx, const float* pts, uint32_t n_pts, const uint32_t* idx,
+                                     uint32_t count, float* out, gtc_stream_t stream);
+
+/* Little-endian binary export of a host buffer: count elements of elem_bytes
+ * (1, 2, 4 or 8) each, written in order as the reference's dump writes its
+ * buffers (write_u32::<LittleEndian> per element, radixsort-vulkan
+ * main.rs:760-769).  append != 0 appends to an existing file. */
+GTC_API gtc_status gtc_export_le(const char* path, const void* host_data, size_t count, int elem_bytes, int append);
+
 /* ------------------------------------------- reference-signature shims --- */
 /* Synchronous host-array versions with the Rust functions' parameter order.
  * They use a process-wide context on device 0. */
