@@ -246,14 +246,20 @@ __device__ __forceinline__ uint32_t third_bits(uint32_t m) {  // morton.rs:62-68
   x = (x ^ (x >> 16)) & 0x000003ffu;
   return x;
 }
+// The 11 bits at positions 0, 3, ..., 30 of a 32-bit word, packed.
+__device__ __forceinline__ uint32_t compact11(uint32_t x) {
+  x &= 0x49249249u;
+  x = (x ^ (x >> 2)) & 0xc30c30c3u;
+  x = (x ^ (x >> 4)) & 0x0f00f00fu;
+  x = (x ^ (x >> 8)) & 0xff0000ffu;
+  x = (x ^ (x >> 16)) & 0x000007ffu;
+  return x;
+}
+// Bits 0, 3, ..., 60 of m (morton.rs:62-68 widened to 21 bits per axis), as
+// two 32-bit halves: bits 0..30 from the low word, bits 33..60 from the high.
 __device__ __forceinline__ uint32_t third_bits(uint64_t m) {
-  uint64_t x = m & 0x1249249249249249ull;
-  x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
-  x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
-  x = (x ^ (x >> 8)) & 0x001f0000ff0000ffull;
-  x = (x ^ (x >> 16)) & 0x001f00000000ffffull;
-  x = (x ^ (x >> 32)) & 0x00000000001fffffull;
-  return (uint32_t)x;
+  const uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
+  return compact11(lo) | (compact11((hi >> 1) & 0x09249249u) << 11);
 }
 
 template <class K, int Q = 0>

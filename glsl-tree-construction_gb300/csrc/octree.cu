@@ -268,9 +268,18 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
                                gtc_octnode* nodes, uint32_t capacity, bool with_leaves) {
   const uint32_t work = d_u ? n_max : u_host;
   if (work == 0) return cudaSuccess;
-  // One resident wave (5 blocks of 256 per SM at 48 registers); each warp
-  // walks many 32-node slices, so the partial batch at its end is small.
-  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)L.num_sms * 5));
+  // One resident wave; each warp walks many 32-node slices, so the partial
+  // batch at its end is small.
+  static int resident[2] = {0, 0};  // blocks per SM of each instantiation, queried once
+  int& occ = resident[with_leaves ? 1 : 0];
+  if (occ == 0) {
+    const void* kern = with_leaves ? (const void*)octree_make_kernel<K, true> : (const void*)octree_make_kernel<K, false>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, OCT_THREADS, 0) != cudaSuccess || occ < 1) {
+      cudaGetLastError();
+      occ = 4;
+    }
+  }
+  const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)(L.num_sms * occ)));
   if (with_leaves)
     octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
                                                                      edge, ps, mn, rg, nodes, capacity,
