@@ -86,6 +86,13 @@ __device__ __forceinline__ uint64_t ld_hint(const uint64_t* p, uint64_t pol) {
   return v;
 }
 
+__device__ __forceinline__ void st_hint(uint32_t* p, uint32_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(uint64_t* p, uint64_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
 // Hint: fetch the 128-byte line holding p into L2.
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 

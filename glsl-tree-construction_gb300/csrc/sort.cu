@@ -179,7 +179,7 @@ struct OnesweepSmem {
   uint32_t tile_id;
 };
 
-template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB, int LBW, bool EARLY>
+template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB, int LBW, bool EARLY, bool L2H = false>
 __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t dmask,
@@ -220,11 +220,23 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   K key[KPT];
   uint32_t val[KPT];
   const uint32_t wbase = tile_base + warp * 32 * KPT + lane;
+  // L2H: the input is read once (evict first); the output, which the next
+  // pass reads, is written evict last so that part of it is still in L2.
+  uint64_t pol_in = 0, pol_out = 0;
+  if (L2H) {
+    pol_in = l2_drop_policy();
+    pol_out = l2_keep_policy();
+  }
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const uint32_t pos = wbase + j * 32;
-    key[j] = (pos < n) ? kin[pos] : ~K(0);
-    if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
+    if (L2H) {
+      key[j] = (pos < n) ? ld_hint(kin + pos, pol_in) : ~K(0);
+      if (HAS_VALS) val[j] = (pos < n) ? ld_hint(vin + pos, pol_in) : 0u;
+    } else {
+      key[j] = (pos < n) ? kin[pos] : ~K(0);
+      if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
+    }
   }
 
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -335,8 +347,13 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   for (uint32_t i = tid; i < valid; i += THREADS) {
     const K k = s.keys[i];
     const uint32_t o = s.global_base[(uint32_t)(k >> shift) & dmask] + i;
-    kout[o] = k;
-    if (HAS_VALS) vout[o] = s.vals[i];
+    if (L2H) {
+      st_hint(kout + o, k, pol_out);
+      if (HAS_VALS) st_hint(vout + o, s.vals[i], pol_out);
+    } else {
+      kout[o] = k;
+      if (HAS_VALS) vout[o] = s.vals[i];
+    }
   }
 }
 
@@ -559,7 +576,7 @@ struct Variant {
 constexpr Variant kVariants[] = {{256, 16, 0, 3, 1}, {384, 16, 0, 2, 1}, {512, 12, 0, 2, 1}, {256, 16, 1, 1, 1},
                                  {256, 16, 2, 1, 1}, {512, 8, 2, 1, 1},  {256, 24, 2, 1, 1}, {256, 16, 0, 4, 1},
                                  {512, 8, 0, 2, 1},  {384, 12, 0, 3, 1}, {256, 16, 0, 3, 0}, {384, 16, 0, 2, 0},
-                                 {512, 12, 0, 2, 0}, {256, 24, 0, 2, 0}};
+                                 {512, 12, 0, 2, 0}, {256, 24, 0, 2, 0}, {256, 16, 4, 3, 1}, {512, 12, 4, 2, 0}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
 static int g_pinned[2] = {-1, -1};  // gtc_sort_set_variant: overrides the tuned choice
@@ -571,12 +588,12 @@ int sort_select_variant(int key_bits, int bits, uint32_t n) {
   return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
 }
 
-template <class K, int THREADS, int KPT, bool HV, int MINB, bool EARLY>
+template <class K, int THREADS, int KPT, bool HV, int MINB, bool EARLY, bool L2H = false>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
                               uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
                               uint32_t* tile_counter) {
   using S = OnesweepSmem<K, THREADS, KPT>;
-  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, EARLY>;
+  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, EARLY, L2H>;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
@@ -618,10 +635,13 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
   // TMA bulk copies need 16-byte aligned sources; other inputs use the
   // one-tile-per-CTA kernel of the same tile width.
   const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
-  if (kVariants[v].kind != 0 && !aligned) v = 0;
+  if ((kVariants[v].kind == 1 || kVariants[v].kind == 2) && !aligned) v = 0;
 #define GTC_OS(T, P, MB, LB)                                                                                   \
   return hv ? launch_one<K, T, P, true, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
             : launch_one<K, T, P, false, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_OSH(T, P, MB, EA)                                                                                  \
+  return hv ? launch_one<K, T, P, true, MB, EA, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
+            : launch_one<K, T, P, false, MB, EA, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
 #define GTC_TMA(T, P, M)                                                                                     \
   return hv ? launch_tma<K, T, P, true, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)    \
             : launch_tma<K, T, P, false, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
@@ -639,9 +659,12 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
     case 10: GTC_OS(256, 16, 3, false);
     case 11: GTC_OS(384, 16, 2, false);
     case 12: GTC_OS(512, 12, 2, false);
-    default: GTC_OS(256, 24, 2, false);
+    case 13: GTC_OS(256, 24, 2, false);
+    case 14: GTC_OSH(256, 16, 3, true);
+    default: GTC_OSH(512, 12, 2, false);
   }
 #undef GTC_OS
+#undef GTC_OSH
 #undef GTC_TMA
 }
 
