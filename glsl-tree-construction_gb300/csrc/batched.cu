@@ -432,45 +432,65 @@ __global__ void bt_cloud_offsets_kernel(uint32_t* uoff, const uint32_t* ne_start
 }
 
 // One octree body: code g of the cloud described by ci.
-__device__ __forceinline__ void bt_octree_one(uint32_t g, uint4 ci, const uint32_t* codes, const uint8_t* prefix_n,
-                                              const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
-                                              const uint32_t* edge, const uint32_t* ps, float mn, float rg,
-                                              gtc_octnode* nodes, uint32_t capacity, uint32_t lmask_keep,
-                                              uint32_t* status) {
-  constexpr int A = KeyTraits<uint32_t>::A;
-  const uint32_t U0 = ci.x, k = g - U0, m = ci.y - U0 - 1, bias = ci.z, O = ci.w;
-  if (O >= capacity) {
-    if (k == 0) atomicOr(status, DEV_CAPACITY);
-    return;
-  }
-  if (m == 0) {
-    octree_root_only<uint32_t>(nodes + O, capacity - O, mn, rg, status);
-    return;
-  }
-  const int root_level = (prefix_n[U0] - A) / 3;
-  octree_make_node<uint32_t, true>(k, codes + U0, prefix_n + U0, hll + U0, hlr + U0, left + U0, edge + U0, ps + U0,
-                                   bias, root_level, mn, rg, nodes + O, capacity - O, lmask_keep, status);
-}
-
 // Octree of every cloud, and the cloud-local node offsets (what the
 // single-cloud node-offset scan gives each cloud).  Warp slices of 32 codes:
 // the slice's cloud comes from one binary search (then a step or two per
 // lane), every lane writes its node offset, and the codes that own octree
-// nodes are compacted into a per-warp queue and processed 32 at a time, as in
-// octree.cu.
-__global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restrict__ codes, const uint32_t* uoff,
-                                                        uint32_t S, const uint4* cinfo, const uint8_t* prefix_n,
-                                                        const uint8_t* hll, const uint8_t* hlr, const int32_t* left,
-                                                        const uint32_t* edge, const uint32_t* ps,
-                                                        uint32_t* node_offsets, float mn, float rg, gtc_octnode* nodes,
-                                                        uint32_t capacity, uint32_t lmask_keep, uint32_t* status) {
-  constexpr int WARPS = 256 / 32;
-  __shared__ uint2 s_queue[WARPS][64];
+// nodes are compacted, with their clouds, into a per-warp queue and run 32
+// at a time through the single-cloud kernel's breadth-first warp batch
+// (octree_warp_batch), each lane with its own cloud.
+constexpr int BT_OCT_THREADS = 256;
+
+__global__ void __launch_bounds__(BT_OCT_THREADS) bt_octree_kernel(const uint32_t* __restrict__ codes,
+                                                                   const uint32_t* uoff, uint32_t S,
+                                                                   const uint4* cinfo, const uint8_t* prefix_n,
+                                                                   const uint8_t* hll, const uint8_t* hlr,
+                                                                   const int32_t* left, const uint32_t* edge,
+                                                                   const uint32_t* ps, uint32_t* node_offsets,
+                                                                   float mn, float rg, gtc_octnode* nodes,
+                                                                   uint32_t capacity, uint32_t lmask_keep,
+                                                                   uint32_t* status) {
+  constexpr int WARPS = BT_OCT_THREADS / 32;
+  constexpr int A = KeyTraits<uint32_t>::A;
+  __shared__ OctWarp s_warp[WARPS];
+  __shared__ uint32_t s_cloud[WARPS][64];
   const uint32_t U = uoff[S];
   const int lane = threadIdx.x & 31;
-  uint2* q = s_queue[threadIdx.x >> 5];
+  OctWarp& Wq = s_warp[threadIdx.x >> 5];
+  uint32_t* qc = s_cloud[threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform
   const uint32_t warps = gridDim.x * WARPS;
+  auto run_batch = [&](uint32_t cnt) {
+    const bool valid = (uint32_t)lane < cnt;
+    const uint32_t g = valid ? Wq.q[lane] : 0u;
+    const uint32_t c = valid ? qc[lane] : 0u;
+    const uint32_t rest_g = (lane + 32 < qn) ? Wq.q[lane + 32] : 0u;
+    const uint32_t rest_c = (lane + 32 < qn) ? qc[lane + 32] : 0u;
+    __syncwarp();
+    if (lane + 32 < qn) {
+      Wq.q[lane] = rest_g;
+      qc[lane] = rest_c;
+    }
+    qn -= cnt;
+    OctCloud cl{0u, 0u, 0u, 0, nodes, 0u};
+    bool ok = valid;
+    if (valid) {
+      const uint4 ci = cinfo[c];
+      cl.u0 = ci.x;
+      cl.mend = ci.y - 1;
+      cl.bias = ci.z;
+      cl.root_level = (prefix_n[ci.x] - A) / 3;
+      if (ci.w >= capacity) {
+        if (g == ci.x) atomicOr(status, DEV_CAPACITY);
+        ok = false;
+      } else {
+        cl.nodes = nodes + ci.w;
+        cl.capacity = capacity - ci.w;
+      }
+    }
+    octree_warp_batch<uint32_t, true>(Wq, ok, g, cl, codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, lmask_keep,
+                                      status);
+  };
   for (uint32_t base = (blockIdx.x * WARPS + (threadIdx.x >> 5)) * 32; base < U; base += warps * 32) {
     const uint32_t g = base + lane;
     bool act = false;
@@ -480,28 +500,26 @@ __global__ void __launch_bounds__(256) bt_octree_kernel(const uint32_t* __restri
       const uint4 ci = cinfo[c];
       const uint32_t k = g - ci.x, m = ci.y - ci.x - 1;
       node_offsets[g] = (k == 0) ? 0u : ps[g] - ci.z;
-      act = (m == 0) ? true : (k < m && (k == 0 || edge[g] > 0));
+      if (m == 0) {  // a cloud of one distinct key: its root alone (D18)
+        if (ci.w < capacity)
+          octree_root_only<uint32_t>(nodes + ci.w, capacity - ci.w, mn, rg, status);
+        else
+          atomicOr(status, DEV_CAPACITY);
+      } else {
+        act = k < m && (k == 0 || edge[g] > 0);
+      }
     }
     const uint32_t bal = __ballot_sync(0xffffffffu, act);
-    if (act) q[qn + __popc(bal & ((1u << lane) - 1u))] = make_uint2(g, c);
+    if (act) {
+      const uint32_t pos = qn + __popc(bal & ((1u << lane) - 1u));
+      Wq.q[pos] = g;
+      qc[pos] = c;
+    }
     qn += __popc(bal);
     __syncwarp();
-    if (qn >= 32) {
-      const uint2 e = q[lane];
-      bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, lmask_keep,
-                    status);
-      const uint2 rest = (lane + 32 < qn) ? q[lane + 32] : make_uint2(0, 0);
-      __syncwarp();
-      if (lane + 32 < qn) q[lane] = rest;
-      qn -= 32;
-      __syncwarp();
-    }
+    if (qn >= 32) run_batch(32u);
   }
-  if (lane < qn) {
-    const uint2 e = q[lane];
-    bt_octree_one(e.x, cinfo[e.y], codes, prefix_n, hll, hlr, left, edge, ps, mn, rg, nodes, capacity, lmask_keep,
-                    status);
-  }
+  if (qn > 0) run_batch(qn);
 }
 
 struct BatchWs {
@@ -668,8 +686,15 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   }
   {
     Stage t(ctx, stream, GTC_STAGE_OCTREE);
-    const uint32_t ogrid = max(1u, min(ceil_div(n_total, 256), (uint32_t)L.num_sms * 5));
-    bt_octree_kernel<<<ogrid, 256, 0, s>>>(out->keys, out->key_offset, S, reinterpret_cast<const uint4*>(W.seg_hist),
+    static int occ = 0;  // resident blocks per SM, queried once
+    if (occ == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bt_octree_kernel, BT_OCT_THREADS, 0) !=
+                         cudaSuccess ||
+                     occ < 1)) {
+      cudaGetLastError();
+      occ = 4;
+    }
+    const uint32_t ogrid = max(1u, min(ceil_div(n_total, BT_OCT_THREADS), (uint32_t)(L.num_sms * occ)));
+    bt_octree_kernel<<<ogrid, BT_OCT_THREADS, 0, s>>>(out->keys, out->key_offset, S, reinterpret_cast<const uint4*>(W.seg_hist),
                                            out->prefix_n, out->has_leaf_left, out->has_leaf_right, out->left_child,
                                            out->edge_count, W.ps, out->node_offsets, min_coord, range, out->nodes,
                                            out->nodes_capacity, leaf_mask_keep(), L.status);
