@@ -301,7 +301,8 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   GTC_TRY(ctx, cudaMemsetAsync(Wk.header, 0, Wk.header_words * 4, S(stream)));
   {
     StageTimer t(ctx, stream, GTC_STAGE_MORTON);
-    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, vals_alt, n, mn, rg, Wk,
+    // No payload written here: the first sort pass makes the iota itself.
+    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, nullptr, n, mn, rg, Wk,
                                        passes));
   }
   bool in_alt = false;  // "alt" here = the caller's keys/idx buffers
@@ -310,7 +311,7 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
     if (ctx->profiling)
       for (int i = 0; i < 2 * passes; ++i) ev.push_back(get_event(ctx));
     GTC_TRY(ctx, launch_onesweep_passes<K>(L, keys_alt, vals_alt, keys, o->idx, n, 0, 3 * B, Wk, passes, &in_alt,
-                                           ev.empty() ? nullptr : ev.data()));
+                                           ev.empty() ? nullptr : ev.data(), -1, true));
     for (int p = 0; p < (int)ev.size() / 2; ++p) ctx->pending.push_back({ev[2 * p], ev[2 * p + 1], GTC_STAGE_ONESWEEP});
   }
   {

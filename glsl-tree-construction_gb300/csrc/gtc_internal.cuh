@@ -401,12 +401,14 @@ template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
                                const SortWorkspace& W, int passes);
 // variant < 0: the pinned variant, else the autotuned one for (key width,
-// bits, n), else the built-in default.
+// bits, n), else the built-in default.  iota_vals: the values' input is the
+// position (vals is still the buffer the payload lives in between passes),
+// made by the first pass instead of read.
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
                                    bool* result_in_alt, cudaEvent_t* ev_pass /* nullable [2*passes] */,
-                                   int variant = -1);
+                                   int variant = -1, bool iota_vals = false);
 // The variant a sort of n keys of key_bits width over `bits` bits will use.
 int sort_select_variant(int key_bits, int bits, uint32_t n);
 // Autotuner cache (tune.cu): the tuned variant for (key width, bits, n), or -1.

@@ -152,14 +152,14 @@ __global__ void __launch_bounds__(THREADS, 2) morton_hist_kernel(const float4* _
     for (int u = 0; u < 4; ++u) {
       const K k = encode_point<K, Q>(p[u], mn, rg, inv_rg);
       keys[i + u * stride] = k;
-      idx[i + u * stride] = (uint32_t)(i + u * stride);
+      if (idx) idx[i + u * stride] = (uint32_t)(i + u * stride);
       hist_add<K>(s_hist, k, 0, end_bit, passes);
     }
   }
   for (; i < n; i += stride) {
     const K k = encode_point<K, Q>(__ldcs(pts + i), mn, rg, inv_rg);
     keys[i] = k;
-    idx[i] = (uint32_t)i;
+    if (idx) idx[i] = (uint32_t)i;
     hist_add<K>(s_hist, k, 0, end_bit, passes);
   }
   hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, s_warp_sums, &s_last);
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
     const uint32_t guess = blockIdx.x * TILE;
     constexpr uint32_t KL = 128 / sizeof(K), VL = 32;  // elements per 128-byte line
     for (uint32_t e = guess + tid * KL; e < guess + TILE && e < n; e += THREADS * KL) prefetch_l2(kin + e);
-    if (HAS_VALS)
+    if (HAS_VALS && vin)
       for (uint32_t e = guess + tid * VL; e < guess + TILE && e < n; e += THREADS * VL) prefetch_l2(vin + e);
   }
   __syncthreads();
@@ -230,12 +230,14 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const uint32_t pos = wbase + j * 32;
+    // Values absent with HAS_VALS: the iota payload (the first pass of a
+    // sort whose values are the input positions).
     if (L2H) {
       key[j] = (pos < n) ? ld_hint(kin + pos, pol_in) : ~K(0);
-      if (HAS_VALS) val[j] = (pos < n) ? ld_hint(vin + pos, pol_in) : 0u;
+      if (HAS_VALS) val[j] = (pos < n) ? (vin ? ld_hint(vin + pos, pol_in) : pos) : 0u;
     } else {
       key[j] = (pos < n) ? kin[pos] : ~K(0);
-      if (HAS_VALS) val[j] = (pos < n) ? vin[pos] : 0u;
+      if (HAS_VALS) val[j] = (pos < n) ? (vin ? vin[pos] : pos) : 0u;
     }
   }
 
@@ -635,7 +637,7 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
   // TMA bulk copies need 16-byte aligned sources; other inputs use the
   // one-tile-per-CTA kernel of the same tile width.
   const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
-  if ((kVariants[v].kind == 1 || kVariants[v].kind == 2) && !aligned) v = 0;
+  if ((kVariants[v].kind == 1 || kVariants[v].kind == 2) && (!aligned || (hv && !vin))) v = 0;
 #define GTC_OS(T, P, MB, LB)                                                                                   \
   return hv ? launch_one<K, T, P, true, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
             : launch_one<K, T, P, false, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
@@ -741,13 +743,13 @@ template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, 
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
-                                   bool* result_in_alt, cudaEvent_t* ev, int variant) {
+                                   bool* result_in_alt, cudaEvent_t* ev, int variant, bool iota_vals) {
   const int v = (variant >= 0 && variant < kNumVariants) ? variant
                                                           : sort_select_variant(8 * sizeof(K), end_bit - begin_bit, n);
   const bool hv = vals != nullptr;
   K* src_k = keys;
   K* dst_k = keys_alt;
-  uint32_t* src_v = vals;
+  uint32_t* src_v = (hv && iota_vals) ? nullptr : vals;  // the first pass makes the iota payload itself
   uint32_t* dst_v = vals_alt;
   for (int p = 0; p < passes; ++p) {
     const int shift = begin_bit + 8 * p;
@@ -761,7 +763,7 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
     K* tk = src_k;
     src_k = dst_k;
     dst_k = tk;
-    uint32_t* tv = src_v;
+    uint32_t* tv = (p == 0 && hv && iota_vals) ? vals : src_v;
     src_v = dst_v;
     dst_v = tv;
   }
@@ -770,10 +772,10 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
 }
 template cudaError_t launch_onesweep_passes<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*, int);
+                                                      cudaEvent_t*, int, bool);
 template cudaError_t launch_onesweep_passes<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*, int);
+                                                      cudaEvent_t*, int, bool);
 
 int sort_num_variants() { return kNumVariants; }
 int sort_get_variant(int key_bits) {
