@@ -373,6 +373,87 @@ __global__ void __launch_bounds__(BU_THREADS) bt_unique_kernel(const uint32_t* k
   if (tid == 0 && base + valid == n) uoff[S] = out0 + total;
 }
 
+// The resident segment form of the same unique (scan.cu's
+// chunk_unique_kernel, out of place): rows of 32 codes per warp; a warp
+// tracks the cloud of its row (one binary search per segment, then a step
+// per cloud start), so the cloud starts of a row come as a bit mask.
+__device__ __forceinline__ uint32_t bt_row_starts(const uint32_t* off, uint32_t S, uint32_t r, uint32_t& cur) {
+  uint32_t smask = (off[cur] == r) ? 1u : 0u;
+  while (cur + 1 < S && off[cur + 1] < r + 32) {
+    ++cur;
+    smask |= 1u << (off[cur] - r);
+  }
+  return smask;
+}
+
+__global__ void __launch_bounds__(CS_THREADS) bt_chunk_unique_kernel(const uint32_t* __restrict__ kin,
+                                                                     const uint32_t* __restrict__ vin,
+                                                                     uint32_t* __restrict__ kout,
+                                                                     uint32_t* __restrict__ vout, uint32_t n,
+                                                                     const uint32_t* off, uint32_t S, uint32_t* uoff,
+                                                                     uint32_t* ws, const uint32_t* bad,
+                                                                     uint32_t* status) {
+  __shared__ uint32_t s_seg[CS_WARPS];
+  __shared__ uint32_t s_red[CS_WARPS];
+  if (*bad) return;  // the same word for every block
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t nseg = gridDim.x * CS_WARPS;
+  const uint64_t SL = (((uint64_t)n + nseg - 1) / nseg + 31) & ~(uint64_t)31;
+  const uint64_t beg64 = (uint64_t)(blockIdx.x * CS_WARPS + warp) * SL;
+  const uint32_t beg = (uint32_t)min(beg64, (uint64_t)n);
+  const uint32_t end = (uint32_t)min(beg64 + SL, (uint64_t)n);
+  const uint32_t c_beg = (beg < end) ? owner(off, S, beg) : 0u;
+  const uint32_t first_prev = (beg > 0 && beg < end) ? kin[beg - 1] : 0u;
+
+  // 1. kept codes per segment
+  uint32_t cnt = 0;
+  {
+    uint32_t carry = first_prev, cur = c_beg;
+    for (uint32_t r = beg; r < end; r += 32) {
+      const uint32_t i = r + lane;
+      const uint32_t key = (i < end) ? kin[i] : 0u;
+      const uint32_t smask = bt_row_starts(off, S, r, cur);
+      uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+      if (lane == 0) prev = carry;
+      const bool keep = i < end && (i == 0 || key != prev || ((smask >> lane) & 1u));
+      cnt += __popc(__ballot_sync(0xffffffffu, keep));
+      carry = __shfl_sync(0xffffffffu, key, 31);
+    }
+  }
+  if (lane == 0) s_seg[warp] = cnt;
+
+  // 2. block prefix
+  uint32_t run = cs_block_prefix(ws + 64, s_seg, s_red, status);
+  run += s_seg[warp];
+
+  // 3. rescan and write; the lane holding a cloud's first code records U_c
+  {
+    uint32_t carry = first_prev, cur = c_beg;
+    for (uint32_t r = beg; r < end; r += 32) {
+      const uint32_t i = r + lane;
+      const uint32_t key = (i < end) ? kin[i] : 0u;
+      const uint32_t val = (i < end) ? vin[i] : 0u;
+      const uint32_t smask = bt_row_starts(off, S, r, cur);
+      uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+      if (lane == 0) prev = carry;
+      const bool start = i < end && ((smask >> lane) & 1u);
+      const bool keep = i < end && (i == 0 || key != prev || start);
+      const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const uint32_t o = run + __popc(bal & lt);
+        kout[o] = key;
+        vout[o] = val;
+        if (start) uoff[owner(off, S, i)] = o;
+      }
+      run += __popc(bal);
+      carry = __shfl_sync(0xffffffffu, key, 31);
+    }
+  }
+  // The last warp of the last block ends at n: its running count is U.
+  if (blockIdx.x == gridDim.x - 1 && warp == CS_WARPS - 1 && lane == 0) uoff[S] = run;
+}
+
 // Empty clouds own no code: their U_c is the next cloud's (one thread; runs
 // from the end, so runs of empty clouds resolve).
 __global__ void bt_uoff_fix_kernel(const uint32_t* off, uint32_t S, uint32_t* uoff, const uint32_t* bad) {
@@ -648,9 +729,25 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
     Stage t(ctx, stream, GTC_STAGE_UNIQUE);
     const uint32_t utiles = ceil_div(n_total, BU_TILE);
     uint32_t* uws = reinterpret_cast<uint32_t*>(W.scan_ws);
-    BCHK(cudaMemsetAsync(uws, 0, (64 + (size_t)utiles) * 4, s));
-    bt_unique_kernel<<<utiles, BU_THREADS, 0, s>>>(src_k, src_v, out->keys, out->idx, n_total, d_offsets, S,
-                                                   out->key_offset, uws, bad, L.status);
+    // The resident segment form once the batch fills the GPU; its
+    // descriptors fit the workspace's tile count.
+    static int occ = 0;  // resident blocks per SM, queried once
+    if (occ == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bt_chunk_unique_kernel, CS_THREADS, 0) !=
+                         cudaSuccess ||
+                     occ < 1)) {
+      cudaGetLastError();
+      occ = 1;
+    }
+    const uint32_t g = min((uint32_t)(occ * L.num_sms), utiles);
+    if (g >= 64 && (uint64_t)n_total >= (uint64_t)g * CS_WARPS * 256) {
+      BCHK(cudaMemsetAsync(uws, 0, (64 + (size_t)g) * 4, s));
+      bt_chunk_unique_kernel<<<g, CS_THREADS, 0, s>>>(src_k, src_v, out->keys, out->idx, n_total, d_offsets, S,
+                                                      out->key_offset, uws, bad, L.status);
+    } else {
+      BCHK(cudaMemsetAsync(uws, 0, (64 + (size_t)utiles) * 4, s));
+      bt_unique_kernel<<<utiles, BU_THREADS, 0, s>>>(src_k, src_v, out->keys, out->idx, n_total, d_offsets, S,
+                                                     out->key_offset, uws, bad, L.status);
+    }
     BCHK(cudaGetLastError());
     bt_uoff_fix_kernel<<<1, 32, 0, s>>>(d_offsets, S, out->key_offset, bad);
     BCHK(cudaGetLastError());

@@ -35,35 +35,6 @@ size_t scan_workspace_bytes(uint32_t n) {
 //      warp-only scans: no block barrier, no staging in shared memory.
 // The single-pass kernels above pay a chained look-back per 4.6K-item tile;
 // here each block waits once.
-constexpr int CS_THREADS = 512;
-constexpr int CS_WARPS = CS_THREADS / 32;
-
-// Exclusive prefix of this block over the descriptors of blocks [0, t), and
-// the block's own segment prefixes (s_seg: per-warp totals in, exclusive
-// prefixes out).  Publishes the block total first.  Returns the prefix.
-__device__ __forceinline__ uint32_t cs_block_prefix(uint32_t* desc, uint32_t* s_seg, uint32_t* s_red,
-                                                    uint32_t* status) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t t = blockIdx.x;
-  __syncthreads();
-  if (warp == 0) {
-    const uint32_t v = (lane < CS_WARPS) ? s_seg[lane] : 0u;
-    const uint32_t inc = warp_inclusive_sum(v);
-    if (lane < CS_WARPS) s_seg[lane] = inc - v;
-    if (lane == 31) st_relaxed(desc + t, (inc << 2) | FLAG_AGGREGATE);
-  }
-  uint32_t acc = 0;
-  for (uint32_t i = tid; i < t; i += CS_THREADS) acc += spin_descriptor(desc + i, status) >> 2;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) s_red[warp] = acc;
-  __syncthreads();
-  uint32_t pre = 0;
-#pragma unroll
-  for (int w = 0; w < CS_WARPS; ++w) pre += s_red[w];
-  return pre;
-}
-
 // Inclusive scan with the node-offset rules of scan_kernel.  Rows of 128
 // items (one uint4 per lane); S is a multiple of 128, so rows never straddle
 // segments and in/out must be 16-byte aligned.
