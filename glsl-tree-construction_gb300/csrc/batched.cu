@@ -23,7 +23,7 @@
 //               edge in each cloud's last slot;
 //   6. one inclusive scan of all edge counts; cloud c's node offsets are the
 //               scan minus its value just before U_c (the bias);
-//   7. octree of each cloud (octree_make_node) into its node range starting
+//   7. octree of each cloud (octree_warp_batch) into its node range starting
 //               at O_c = (non-empty clouds before c) + bias.
 
 #include <utility>
