@@ -1,6 +1,7 @@
 // api.cu - the C ABI (include/gtc.h): context, workspace, stage operators,
 // the fused stream-ordered pipeline and its host-buffer form.
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -660,6 +661,17 @@ GTC_API gtc_status gtc_build_octree(gtc_ctx* ctx, const float* pts, uint32_t n, 
   return pipeline<uint64_t>(ctx, pts, n, mn, rg, out, ws, wsb, s);
 }
 
+// The device address of page-locked host memory (cudaHostAlloc /
+// cudaHostRegister), or null for any other pointer.
+static const void* device_view(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, uint32_t n, float mn, float rg,
                                          int key_bits, gtc_octnode* host_nodes, uint32_t host_cap,
                                          uint32_t* host_counts) {
@@ -675,12 +687,17 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
   cudaStream_t st = ctx->own_stream;
   gtc_status s = ensure_resident(ctx, n, key_bits, 0);
   if (s != GTC_OK) return s;
+  // Page-locked input is streamed from host memory by the Morton pass itself,
+  // so the transfer overlaps the encoding; other host memory is copied first.
+  const float* d_in = reinterpret_cast<const float*>(device_view(host_pts));
+  if (d_in && (reinterpret_cast<uintptr_t>(d_in) & 15) != 0) d_in = nullptr;
   for (int attempt = 0; attempt < 2; ++attempt) {
     Resident& r = ctx->res;
-    GTC_TRY(ctx, cudaMemcpyAsync(r.pts, host_pts, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+    if (!d_in) GTC_TRY(ctx, cudaMemcpyAsync(r.pts, host_pts, (size_t)n * 16, cudaMemcpyHostToDevice, st));
     gtc_octree_buffers b{r.keys, r.idx, r.prefix_n, r.hll, r.hlr, r.left, r.parent, r.edge, r.ps, r.nodes,
                          r.nodes_cap, r.counts};
-    s = gtc_build_octree(ctx, reinterpret_cast<const float*>(r.pts), n, mn, rg, key_bits, &b, r.ws, r.ws_bytes, st);
+    s = gtc_build_octree(ctx, d_in ? d_in : reinterpret_cast<const float*>(r.pts), n, mn, rg, key_bits, &b, r.ws,
+                         r.ws_bytes, st);
     if (s != GTC_OK) return s;
     uint32_t c[4];
     GTC_TRY(ctx, cudaMemcpyAsync(c, r.counts, 16, cudaMemcpyDeviceToHost, st));

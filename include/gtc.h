@@ -245,7 +245,10 @@ GTC_API gtc_status gtc_build_octree(gtc_ctx* ctx, const float* pts, uint32_t n, 
 /* The same from HOST buffers: copies pts in, builds on the context's own
  * resident buffers, copies the o octree nodes out (host_nodes holds
  * host_nodes_capacity nodes) and host_counts[0..2] = u, m, o.  Synchronous.
- * Host buffers should be pinned (cudaHostAlloc) for full copy bandwidth. */
+ * Page-locked points (cudaHostAlloc / gtc_host_alloc) are read by the Morton
+ * pass straight from host memory; other host memory is copied first.  The
+ * nodes are copied back.  If o > host_nodes_capacity the call returns
+ * GTC_ERR_CAPACITY with host_counts set and no nodes copied. */
 GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, uint32_t n, float min_coord,
                                          float range, int key_bits, gtc_octnode* host_nodes,
                                          uint32_t host_nodes_capacity, uint32_t* host_counts);

@@ -116,6 +116,37 @@ def test_host_buffer_entry_point(ctx, oracle):
     assert np.array_equal(nodes[: counts[2]].view(np.int32), exp["nodes"].view(np.int32))
 
 
+def test_host_entry_point_pinned_buffers(ctx, oracle):
+    """Page-locked points take the direct path (the Morton pass reads them in
+    host memory); same result, and a node buffer that is too small is
+    reported with the counts still set."""
+    import ctypes
+
+    L = ctx.L
+    pts = W.config2_points(1 << 19, seed=3)
+    exp, _ = oracle.build_octree(pts, 64, threads=8)
+    o = exp["n_oct_nodes"]
+    hp, hn = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(L.gtc_host_alloc(ctypes.byref(hp), pts.nbytes))
+    ctx.check(L.gtc_host_alloc(ctypes.byref(hn), (o + 16) * 64))
+    try:
+        ctypes.memmove(hp, pts.ctypes.data, pts.nbytes)
+        counts = np.zeros(3, np.uint32)
+        cp = counts.ctypes.data_as(ctypes.c_void_p)
+        ctx.check(L.gtc_build_octree_host(ctx.h, hp, pts.shape[0], 0.0, 1024.0, 64, hn, o + 16, cp))
+        assert tuple(counts) == (exp["n_unique"], exp["n_brt_nodes"], o)
+        got = np.ctypeslib.as_array((ctypes.c_int32 * (o * 16)).from_address(hn.value)).reshape(o, 16)
+        assert np.array_equal(got, exp["nodes"].view(np.int32).reshape(o, 16))
+        counts[:] = 0
+        s = L.gtc_build_octree_host(ctx.h, hp, pts.shape[0], 0.0, 1024.0, 64, hn, o // 2, cp)
+        assert s == 7  # GTC_ERR_CAPACITY
+        assert int(counts[2]) == o
+        ctx.device_status()  # the context stays usable
+    finally:
+        L.gtc_host_free(hp)
+        L.gtc_host_free(hn)
+
+
 def test_deterministic_across_runs(ctx):
     import gtc
     import torch
