@@ -78,38 +78,40 @@ __device__ __forceinline__ uint32_t tw_byte(uint32_t w0, uint32_t w1, uint32_t w
   return (w >> ((j & 3) * 8)) & 0xffu;
 }
 
-// The stack pass for nearest smaller values over this lane's chunk.  The
-// stack is a 16-bit mask of chunk positions (prefix lengths increase from
-// bottom to top; equal lengths never meet on it for distinct keys).  Result
-// per split, one byte: left answer in the chunk (15 = none) << 4 | right
-// answer (0 = none).  Boundaries (0) pop everything and stay at the bottom.
+// Nearest smaller values inside this lane's chunk of 16 prefix lengths,
+// without a stack: for each position j, one 4-byte SIMD compare per word
+// (__vcmpltu4) marks the positions whose value is below d[j], and the
+// nearest marked position on each side is a bit scan.  Every lane does the
+// same work (a stack pass pops a data-dependent number of entries per step,
+// which diverges across the warp).  Result per split, one byte: left answer
+// in the chunk (15 = none) << 4 | right answer (0 = none).  Equal lengths
+// never face each other across larger ones for distinct keys, so strictly
+// smaller and smaller-or-equal give the same answers; boundaries (0) have
+// no answers of their own and are never queried.
 __device__ __forceinline__ void tw_chunk_stack(TwSmem& s, int chunk) {
   const uint4 dv = *reinterpret_cast<const uint4*>(s.d + TW_H + chunk * TW_C);
-  uint32_t mask = 0;
-  uint64_t lbits = 0, rbits = 0;
-#pragma unroll
-  for (int j = 0; j < TW_C; ++j) {
-    const uint32_t t = tw_byte(dv.x, dv.y, dv.z, dv.w, j);
-    while (mask) {
-      const int top = 31 - __clz(mask);
-      if (tw_byte(dv.x, dv.y, dv.z, dv.w, top) <= t) break;
-      rbits |= (uint64_t)j << (4 * top);
-      mask &= ~(1u << top);
-    }
-    const uint64_t l = mask ? (uint64_t)(31 - __clz(mask)) : 15u;
-    lbits |= l << (4 * j);
-    mask |= 1u << j;
-  }
+  const uint32_t w[4] = {dv.x, dv.y, dv.z, dv.w};
   uint32_t out[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    uint32_t w = 0;
+    uint32_t o = 0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int j = 4 * q + b;
-      w |= (uint32_t)((((lbits >> (4 * j)) & 15u) << 4) | ((rbits >> (4 * j)) & 15u)) << (8 * b);
+      const uint32_t tt = ((w[q] >> (8 * b)) & 0xffu) * 0x01010101u;
+      uint32_t m = 0;  // bit i: d[i] < d[j]
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t c = __vcmpltu4(w[k], tt) & 0x01010101u;
+        m |= ((c * 0x01020408u) >> 24) << (4 * k);
+      }
+      const uint32_t lm = m & ((1u << j) - 1u);
+      const uint32_t rm = m & ~((2u << j) - 1u);
+      const uint32_t l = lm ? (uint32_t)(31 - __clz(lm)) : 15u;
+      const uint32_t r = rm ? (uint32_t)(__ffs(rm) - 1) : 0u;
+      o |= ((l << 4) | r) << (8 * b);
     }
-    out[q] = w;
+    out[q] = o;
   }
   *reinterpret_cast<uint4*>(s.lr + chunk * TW_C) = make_uint4(out[0], out[1], out[2], out[3]);
 }
