@@ -16,8 +16,8 @@
 // key array, and pairs that straddle two clouds, read as 0: smaller than any
 // real prefix length), then answers the nearest-smaller queries in three
 // tiers, none of which loops over a node's range:
-//   1. every lane runs the stack algorithm over its own chunk of 16 splits
-//      (the same work on every lane); about 80% of the answers are inside the
+//   1. every lane answers the queries inside its own chunk of 16 splits
+//      with byte-parallel compares (the same work on every lane); about 80% of the answers are inside the
 //      chunk;
 //   2. the rest are found through two threshold tables: for every value v,
 //      which of a warp-block's 32 chunks has a minimum below v, and which of
@@ -34,7 +34,7 @@
 namespace gtc {
 
 constexpr int TW_THREADS = 512;
-constexpr int TW_C = 16;                   // splits per chunk (one lane's stack pass)
+constexpr int TW_C = 16;                   // splits per chunk (one lane's in-chunk pass)
 constexpr int TW_T = TW_THREADS * TW_C;    // 8192 splits per block
 constexpr int TW_H = 1024;                 // halo on each side
 constexpr int TW_W = TW_T + 2 * TW_H;      // 10240 window positions
@@ -72,43 +72,46 @@ struct TwSmem {
   uint32_t c_first, nb;
 };
 
-// Byte j (0..15) of four little-endian words, j known only at run time.
-__device__ __forceinline__ uint32_t tw_byte(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int j) {
-  const uint32_t w = j < 8 ? (j < 4 ? w0 : w1) : (j < 12 ? w2 : w3);
-  return (w >> ((j & 3) * 8)) & 0xffu;
+// Bytes of a word below t (prefix lengths < 128): bit 7 of each byte of
+// (w | 0x80) - t is clear exactly where the byte is below t.
+__device__ __forceinline__ uint32_t tw_below(uint32_t w, uint32_t tt) {
+  return ~((w | 0x80808080u) - tt) & 0x80808080u;
 }
 
 // Nearest smaller values inside this lane's chunk of 16 prefix lengths,
-// without a stack: for each position j, one 4-byte SIMD compare per word
-// (__vcmpltu4) marks the positions whose value is below d[j], and the
-// nearest marked position on each side is a bit scan.  Every lane does the
-// same work (a stack pass pops a data-dependent number of entries per step,
-// which diverges across the warp).  Result per split, one byte: left answer
-// in the chunk (15 = none) << 4 | right answer (0 = none).  Equal lengths
-// never face each other across larger ones for distinct keys, so strictly
-// smaller and smaller-or-equal give the same answers; boundaries (0) have
-// no answers of their own and are never queried.
+// without a stack (a stack pass pops a data-dependent number of entries per
+// step, which diverges across the warp).  The chunk is transposed so that
+// word k holds positions k, k + 4, k + 8, k + 12; position p = 4b + k then
+// sits at bit 8b + k of a 32-bit mask, and bit order follows position
+// order.  Four tw_below give the mask of every position below d[j], and the
+// nearest on each side is a bit scan.  Result per split, one byte: left
+// answer in the chunk (15 = none) << 4 | right answer (0 = none).  Equal
+// lengths never face each other across larger ones for distinct keys, so
+// strictly smaller and smaller-or-equal give the same answers; boundaries
+// (0) have no answers of their own and are never queried.
 __device__ __forceinline__ void tw_chunk_stack(TwSmem& s, int chunk) {
   const uint4 dv = *reinterpret_cast<const uint4*>(s.d + TW_H + chunk * TW_C);
-  const uint32_t w[4] = {dv.x, dv.y, dv.z, dv.w};
+  const uint32_t a01 = __byte_perm(dv.x, dv.y, 0x5140), a23 = __byte_perm(dv.z, dv.w, 0x5140);
+  const uint32_t c01 = __byte_perm(dv.x, dv.y, 0x7362), c23 = __byte_perm(dv.z, dv.w, 0x7362);
+  const uint32_t wt[4] = {__byte_perm(a01, a23, 0x5410), __byte_perm(a01, a23, 0x7632), __byte_perm(c01, c23, 0x5410),
+                          __byte_perm(c01, c23, 0x7632)};
+  const uint32_t dw[4] = {dv.x, dv.y, dv.z, dv.w};
   uint32_t out[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     uint32_t o = 0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      const int j = 4 * q + b;
-      const uint32_t tt = ((w[q] >> (8 * b)) & 0xffu) * 0x01010101u;
-      uint32_t m = 0;  // bit i: d[i] < d[j]
+      const int bj = 8 * q + b;  // bit of position 4q + b
+      const uint32_t tt = ((dw[q] >> (8 * b)) & 0xffu) * 0x01010101u;
+      uint32_t m = 0;  // bit 8b' + k: d[4b' + k] < d[4q + b]
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const uint32_t c = __vcmpltu4(w[k], tt) & 0x01010101u;
-        m |= ((c * 0x01020408u) >> 24) << (4 * k);
-      }
-      const uint32_t lm = m & ((1u << j) - 1u);
-      const uint32_t rm = m & ~((2u << j) - 1u);
-      const uint32_t l = lm ? (uint32_t)(31 - __clz(lm)) : 15u;
-      const uint32_t r = rm ? (uint32_t)(__ffs(rm) - 1) : 0u;
+      for (int k = 0; k < 4; ++k) m |= tw_below(wt[k], tt) >> (7 - k);
+      const uint32_t lm = m & ((1u << bj) - 1u);
+      const uint32_t rm = m & ~((2u << bj) - 1u);
+      const uint32_t lb = 31 - __clz(lm), rb = __ffs(rm) - 1;
+      const uint32_t l = lm ? 4 * (lb >> 3) + (lb & 7) : 15u;
+      const uint32_t r = rm ? 4 * (rb >> 3) + (rb & 7) : 0u;
       o |= ((l << 4) | r) << (8 * b);
     }
     out[q] = o;
@@ -138,11 +141,11 @@ __device__ __forceinline__ int tw_first_below(const uint8_t* p, uint32_t t) {
   const uint32_t tt = t * 0x01010101u;
   uint32_t c;
   int base;
-  if ((c = __vcmpltu4(q.x, tt))) base = 0;
-  else if ((c = __vcmpltu4(q.y, tt))) base = 4;
-  else if ((c = __vcmpltu4(q.z, tt))) base = 8;
+  if ((c = tw_below(q.x, tt))) base = 0;
+  else if ((c = tw_below(q.y, tt))) base = 4;
+  else if ((c = tw_below(q.z, tt))) base = 8;
   else {
-    c = __vcmpltu4(q.w, tt);
+    c = tw_below(q.w, tt);
     base = 12;
   }
   return base + ((__ffs(c) - 1) >> 3);
@@ -152,11 +155,11 @@ __device__ __forceinline__ int tw_last_below(const uint8_t* p, uint32_t t) {
   const uint32_t tt = t * 0x01010101u;
   uint32_t c;
   int base;
-  if ((c = __vcmpltu4(q.w, tt))) base = 12;
-  else if ((c = __vcmpltu4(q.z, tt))) base = 8;
-  else if ((c = __vcmpltu4(q.y, tt))) base = 4;
+  if ((c = tw_below(q.w, tt))) base = 12;
+  else if ((c = tw_below(q.z, tt))) base = 8;
+  else if ((c = tw_below(q.y, tt))) base = 4;
   else {
-    c = __vcmpltu4(q.x, tt);
+    c = tw_below(q.x, tt);
     base = 0;
   }
   return base + ((31 - __clz(c)) >> 3);
@@ -299,12 +302,39 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
   const int w0 = t0 - TW_H;
 
   // 1. prefix lengths of the window's pairs.
-#pragma unroll 4
-  for (int i = tid; i < TW_W; i += TW_THREADS) {
-    const int x = w0 + i;
+  // Four adjacent pairs per thread and step: five codes (two 16-byte loads
+  // and one more) give four lengths, stored as one word.
+  const bool vec = (reinterpret_cast<uintptr_t>(codes) & 15) == 0;
+#pragma unroll
+  for (int g = tid; g < TW_W / 4; g += TW_THREADS) {
+    const int x = w0 + 4 * g;
     uint32_t v = 0;
-    if (x >= 0 && x < (int)P) v = (uint32_t)delta_key(__ldg(codes + x), __ldg(codes + x + 1));
-    s.d[i] = (uint8_t)v;
+    if (vec && x >= 0 && x + 4 <= (int)P) {
+      K c[5];
+      if (sizeof(K) == 8) {
+        const uint4 q0 = __ldg(reinterpret_cast<const uint4*>(codes + x));
+        const uint4 q1 = __ldg(reinterpret_cast<const uint4*>(codes + x + 2));
+        c[0] = (K)(q0.x | ((uint64_t)q0.y << 32));
+        c[1] = (K)(q0.z | ((uint64_t)q0.w << 32));
+        c[2] = (K)(q1.x | ((uint64_t)q1.y << 32));
+        c[3] = (K)(q1.z | ((uint64_t)q1.w << 32));
+      } else {
+        const uint4 q0 = __ldg(reinterpret_cast<const uint4*>(codes + x));
+        c[0] = (K)q0.x;
+        c[1] = (K)q0.y;
+        c[2] = (K)q0.z;
+        c[3] = (K)q0.w;
+      }
+      c[4] = __ldg(codes + x + 4);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) v |= (uint32_t)delta_key(c[e], c[e + 1]) << (8 * e);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (x + e >= 0 && x + e < (int)P)
+          v |= (uint32_t)delta_key(__ldg(codes + x + e), __ldg(codes + x + e + 1)) << (8 * e);
+    }
+    reinterpret_cast<uint32_t*>(s.d)[g] = v;
   }
   if (SEG) {
     if (tid == 0) {
@@ -332,7 +362,7 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
   }
   __syncthreads();
 
-  // 3. the two threshold tables, and the per-lane stack pass.  A table row
+  // 3. the two threshold tables, and the per-lane in-chunk pass.  A table row
   // for threshold v is the OR of the bits of every entry whose minimum is
   // below v: each entry ORs its bit into row min + 1, then a prefix-OR over
   // the 64 rows (two per lane) completes them.
