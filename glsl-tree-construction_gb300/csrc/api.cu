@@ -158,7 +158,8 @@ size_t pipeline_ws_bytes(uint32_t n) {
   size_t b = align_up((size_t)n * sizeof(K), 256);   // keys_alt
   b += align_up((size_t)n * 4, 256);                  // vals_alt
   b += sort_workspace_bytes(n, passes, 0);
-  b += scan_workspace_bytes(n);
+  b += 2 * scan_workspace_bytes(n);                   // unique, node offsets
+  b += 256;                                           // long-range split count
   return b;
 }
 
@@ -294,16 +295,31 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   w += align_up((size_t)n * 4, 256);
   void* sort_ws = w;
   w += sort_workspace_bytes(n, passes, 0);
-  void* scan_ws = w;
+  void* unique_ws = w;
+  w += scan_workspace_bytes(n);
+  void* offsets_ws = w;
+  w += scan_workspace_bytes(n);
+  uint32_t* q_count = reinterpret_cast<uint32_t*>(w);
+  w += 256;
   K* keys = reinterpret_cast<K*>(o->keys);
   const SortWorkspace Wk = carve_sort_workspace(sort_ws, n, passes, 0);
+  // The Morton pass zeroes the sort's look-back descriptors and, in the same
+  // sweep, the unique / node-offset / queue workspaces behind them, so no
+  // memset node sits between the kernels of the build.
+  SortWorkspace Wz = Wk;
+  Wz.desc_words = (size_t)(reinterpret_cast<uint32_t*>(w) - Wk.desc);
+  // Every kernel after the first starts under a programmatic dependent
+  // launch (not while stage events are being recorded between them).
+  Launch Lp = L;
+  Lp.pdl = !ctx->profiling;
+  Lp.ws_zeroed = true;
 
   GTC_TRY(ctx, cudaMemsetAsync(o->counts, 0, 16, S(stream)));
   GTC_TRY(ctx, cudaMemsetAsync(Wk.header, 0, Wk.header_words * 4, S(stream)));
   {
     StageTimer t(ctx, stream, GTC_STAGE_MORTON);
     // No payload written here: the first sort pass makes the iota itself.
-    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, nullptr, n, mn, rg, Wk,
+    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, nullptr, n, mn, rg, Wz,
                                        passes));
   }
   bool in_alt = false;  // "alt" here = the caller's keys/idx buffers
@@ -311,32 +327,33 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
     std::vector<cudaEvent_t> ev;
     if (ctx->profiling)
       for (int i = 0; i < 2 * passes; ++i) ev.push_back(get_event(ctx));
-    GTC_TRY(ctx, launch_onesweep_passes<K>(L, keys_alt, vals_alt, keys, o->idx, n, 0, 3 * B, Wk, passes, &in_alt,
+    GTC_TRY(ctx, launch_onesweep_passes<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, 0, 3 * B, Wk, passes, &in_alt,
                                            ev.empty() ? nullptr : ev.data(), -1, true));
     for (int p = 0; p < (int)ev.size() / 2; ++p) ctx->pending.push_back({ev[2 * p], ev[2 * p + 1], GTC_STAGE_ONESWEEP});
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_UNIQUE);
     if (in_alt)  // sorted data already in the caller's buffers: in place
-      GTC_TRY(ctx, launch_unique<K>(L, keys, o->idx, keys, o->idx, n, o->counts + 0, scan_ws));
+      GTC_TRY(ctx, launch_unique<K>(Lp, keys, o->idx, keys, o->idx, n, o->counts + 0, unique_ws));
     else
-      GTC_TRY(ctx, launch_unique<K>(L, keys_alt, vals_alt, keys, o->idx, n, o->counts + 0, scan_ws));
+      GTC_TRY(ctx, launch_unique<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, o->counts + 0, unique_ws));
   }
   {
     // vals_alt is free once unique has compacted: it holds the queue of
-    // long-range splits; a spare word of the scan workspace counts them.
+    // long-range splits.
     StageTimer t(ctx, stream, GTC_STAGE_RADIX_TREE);
-    GTC_TRY(ctx, launch_radix_tree<K>(L, keys, o->counts + 0, 0, n, o->prefix_n, o->has_leaf_left, o->has_leaf_right,
-                                      o->left_child, o->parent, o->edge_count, o->counts + 1, vals_alt,
-                                      reinterpret_cast<uint32_t*>(scan_ws) + 32));
+    GTC_TRY(ctx, launch_radix_tree<K>(Lp, keys, o->counts + 0, 0, n, o->prefix_n, o->has_leaf_left,
+                                      o->has_leaf_right, o->left_child, o->parent, o->edge_count, o->counts + 1,
+                                      vals_alt, q_count));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_PREFIX_SUM);
-    GTC_TRY(ctx, launch_node_offsets(L, o->edge_count, o->node_offsets, o->counts + 0, 0, n, o->counts + 2, scan_ws));
+    GTC_TRY(ctx, launch_node_offsets(Lp, o->edge_count, o->node_offsets, o->counts + 0, 0, n, o->counts + 2,
+                                     offsets_ws));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_OCTREE);
-    GTC_TRY(ctx, launch_octree_make<K>(L, keys, o->counts + 0, 0, n, o->prefix_n, o->has_leaf_left,
+    GTC_TRY(ctx, launch_octree_make<K>(Lp, keys, o->counts + 0, 0, n, o->prefix_n, o->has_leaf_left,
                                        o->has_leaf_right, o->left_child, o->edge_count, o->node_offsets, mn, rg,
                                        o->nodes, o->nodes_capacity, true));
   }

@@ -1,6 +1,8 @@
 // gtc_internal.cuh - shared device helpers and launcher declarations.
 #pragma once
 
+#include <utility>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -364,7 +366,43 @@ struct Launch {
   // nonzero (a decision taken on the device, e.g. the learned sort's
   // fallback), so a stream or graph can hold them unconditionally.
   const uint32_t* run_if = nullptr;
+  // Programmatic dependent launch: the kernel's blocks may be scheduled
+  // while the previous kernel of the stream drains; each kernel calls
+  // griddep_wait() before its first global memory access, so only the launch
+  // and block start-up overlap.
+  bool pdl = false;
+  // The unique / scan / tree-queue workspaces of this launch were zeroed by
+  // an earlier kernel of the stream: no memset node in front of them.
+  bool ws_zeroed = false;
 };
+
+// Start of every kernel that may run under a programmatic dependent launch:
+// wait until the previous grid has completed and its writes are visible
+// (a no-op for a normal launch), then let the next grid's blocks be
+// scheduled.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Kernel launch honouring Launch::pdl (cudaLaunchKernelEx with the
+// programmatic stream serialization attribute).
+template <class... P, class... A>
+cudaError_t launch_kernel(const Launch& L, void (*kern)(P...), dim3 grid, dim3 block, size_t smem, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute at[1];
+  if (L.pdl) {
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
 
 // Sort tuning knobs, chosen from the compiled variant table.
 struct SortConfig {

@@ -23,6 +23,7 @@ __global__ void __launch_bounds__(OCT_THREADS) octree_make_kernel(const K* __res
                                                                   const uint32_t* __restrict__ ps, float mn, float rg,
                                                                   gtc_octnode* __restrict__ nodes, uint32_t capacity,
                                                                   uint32_t lmask_keep, uint32_t* status) {
+  griddep_wait();
   constexpr int A = KeyTraits<K>::A;
   constexpr int WARPS = OCT_THREADS / 32;
   __shared__ OctWarp s_warp[WARPS];
@@ -82,14 +83,10 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
   }
   const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)(L.num_sms * occ)));
   if (with_leaves)
-    octree_make_kernel<K, true><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
-                                                                     edge, ps, mn, rg, nodes, capacity,
-                                                                     leaf_mask_keep(), L.status);
-  else
-    octree_make_kernel<K, false><<<grid, OCT_THREADS, 0, L.stream>>>(codes, d_u, u_host, prefix_n, hll, hlr, left,
-                                                                      edge, ps, mn, rg, nodes, capacity, 0xffu,
-                                                                      L.status);
-  return cudaGetLastError();
+    return launch_kernel(L, octree_make_kernel<K, true>, grid, OCT_THREADS, 0, codes, d_u, u_host, prefix_n, hll, hlr,
+                         left, edge, ps, mn, rg, nodes, capacity, leaf_mask_keep(), L.status);
+  return launch_kernel(L, octree_make_kernel<K, false>, grid, OCT_THREADS, 0, codes, d_u, u_host, prefix_n, hll, hlr,
+                       left, edge, ps, mn, rg, nodes, capacity, 0xffu, L.status);
 }
 template cudaError_t launch_octree_make<uint32_t>(const Launch&, const uint32_t*, const uint32_t*, uint32_t, uint32_t,
                                                   const uint8_t*, const uint8_t*, const uint8_t*, const int32_t*,

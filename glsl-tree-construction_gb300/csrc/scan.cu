@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_scan_kernel(const uint32_t* 
                                                                 uint32_t* __restrict__ out, uint32_t count_host,
                                                                 const uint32_t* d_u, int node_offsets, uint32_t* ws,
                                                                 uint32_t* d_o, uint32_t* status) {
+  griddep_wait();
   __shared__ uint32_t s_seg[CS_WARPS];
   __shared__ uint32_t s_red[CS_WARPS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __res
                                                                   K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                                   uint32_t n, uint32_t* ws, uint32_t* d_count,
                                                                   uint32_t* status) {
+  griddep_wait();
   __shared__ uint32_t s_seg[CS_WARPS];
   __shared__ uint32_t s_red[CS_WARPS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -257,6 +259,7 @@ template <class K, bool HAS_VALS>
 __global__ void __launch_bounds__(SCAN_THREADS) unique_kernel(const K* kin, const uint32_t* vin, K* kout,
                                                               uint32_t* vout, uint32_t n, uint32_t* ws,
                                                               uint32_t* d_count, uint32_t* status) {
+  griddep_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   UniqueSmem<K>& s = *reinterpret_cast<UniqueSmem<K>*>(smem_raw);
   uint32_t* desc = ws + 64;
@@ -339,7 +342,7 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
                           uint32_t* d_count, void* ws) {
   uint32_t* w = reinterpret_cast<uint32_t*>(ws);
   const uint32_t tiles = ceil_div(n, SCAN_TILE);
-  cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
+  cudaError_t e = L.ws_zeroed ? cudaSuccess : cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
   if (e != cudaSuccess) return e;
   if (n == 0) return d_count ? cudaMemsetAsync(d_count, 0, 4, L.stream) : cudaSuccess;
   if (kin != kout && vin != vout) {
@@ -349,11 +352,10 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
     const uint32_t g = chunk_grid(L, kern, n, &grid[hv]);
     if (g) {
       if (vin)
-        chunk_unique_kernel<K, true><<<g, CS_THREADS, 0, L.stream>>>(kin, vin, kout, vout, n, w, d_count, L.status);
-      else
-        chunk_unique_kernel<K, false><<<g, CS_THREADS, 0, L.stream>>>(kin, nullptr, kout, nullptr, n, w, d_count,
-                                                                       L.status);
-      return cudaGetLastError();
+        return launch_kernel(L, chunk_unique_kernel<K, true>, g, CS_THREADS, 0, kin, vin, kout, vout, n, w, d_count,
+                             L.status);
+      return launch_kernel(L, chunk_unique_kernel<K, false>, g, CS_THREADS, 0, kin, nullptr, kout, nullptr, n, w,
+                           d_count, L.status);
     }
   }
   const size_t smem = sizeof(UniqueSmem<K>);
@@ -365,7 +367,7 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
       if (e != cudaSuccess) return e;
       attr_set[1] = true;
     }
-    kern<<<tiles, SCAN_THREADS, smem, L.stream>>>(kin, vin, kout, vout, n, w, d_count, L.status);
+    return launch_kernel(L, kern, tiles, SCAN_THREADS, smem, kin, vin, kout, vout, n, w, d_count, L.status);
   } else {
     auto kern = unique_kernel<K, false>;
     if (!attr_set[0]) {
@@ -373,9 +375,8 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
       if (e != cudaSuccess) return e;
       attr_set[0] = true;
     }
-    kern<<<tiles, SCAN_THREADS, smem, L.stream>>>(kin, nullptr, kout, nullptr, n, w, d_count, L.status);
+    return launch_kernel(L, kern, tiles, SCAN_THREADS, smem, kin, nullptr, kout, nullptr, n, w, d_count, L.status);
   }
-  return cudaGetLastError();
 }
 template cudaError_t launch_unique<uint32_t>(const Launch&, const uint32_t*, const uint32_t*, uint32_t*, uint32_t*,
                                              uint32_t, uint32_t*, void*);
@@ -396,6 +397,7 @@ struct ScanSmem {
 __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(const uint32_t* in, uint32_t* out, uint32_t count_host,
                                                             const uint32_t* d_u, int node_offsets, uint32_t* ws,
                                                             uint32_t* d_o, uint32_t* status) {
+  griddep_wait();
   __shared__ ScanSmem s;
   uint32_t* desc = ws + 64;
   const int tid = threadIdx.x;
@@ -459,16 +461,16 @@ static cudaError_t launch_scan(const Launch& L, const uint32_t* in, uint32_t* ou
                                const uint32_t* d_u, uint32_t n_max, int node_offsets, uint32_t* d_o, void* ws) {
   uint32_t* w = reinterpret_cast<uint32_t*>(ws);
   const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);
-  cudaError_t e = cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
+  cudaError_t e = L.ws_zeroed ? cudaSuccess : cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
   if (e != cudaSuccess) return e;
   static uint32_t grid = ~0u;
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
   const uint32_t g = aligned ? chunk_grid(L, (const void*)chunk_scan_kernel, n_max, &grid) : 0u;
   if (g)
-    chunk_scan_kernel<<<g, CS_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
-  else
-    scan_kernel<<<tiles, SCAN_THREADS, 0, L.stream>>>(in, out, count_host, d_u, node_offsets, w, d_o, L.status);
-  return cudaGetLastError();
+    return launch_kernel(L, chunk_scan_kernel, g, CS_THREADS, 0, in, out, count_host, d_u, node_offsets, w, d_o,
+                         L.status);
+  return launch_kernel(L, scan_kernel, tiles, SCAN_THREADS, 0, in, out, count_host, d_u, node_offsets, w, d_o,
+                       L.status);
 }
 
 cudaError_t launch_inclusive_scan(const Launch& L, const uint32_t* in, uint32_t* out, uint32_t n, void* ws) {

@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(THREADS, 2) morton_hist_kernel(const float4* _
                                                               uint32_t* counts,
                                                               uint32_t* bin_offsets, uint32_t* done,
                                                               uint32_t* zero_ptr, size_t zero_words) {
+  griddep_wait();
   __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
   __shared__ uint32_t s_warp_sums[8];
   __shared__ uint32_t s_last;
@@ -188,6 +189,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
                                                            uint32_t* __restrict__ tile_counter,
                                                            uint32_t* __restrict__ status,
                                                            const uint32_t* run_if) {
+  griddep_wait();
   if (run_if && *run_if == 0) return;
   using S = OnesweepSmem<K, THREADS, KPT>;
   constexpr int WARPS = S::WARPS;
@@ -412,6 +414,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tm
                                                                uint32_t* __restrict__ tile_counter,
                                                                uint32_t* __restrict__ status,
                                                                const uint32_t* run_if) {
+  griddep_wait();
   if (run_if && *run_if == 0) return;
   using S = TmaSmem<K, THREADS, KPT, HV>;
   constexpr int TILE = S::TILE;
@@ -603,9 +606,8 @@ static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin
     attr_set = true;
   }
   const uint32_t tiles = ceil_div(n, S::TILE);
-  kern<<<tiles, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
-                                                L.status, L.run_if);
-  return cudaGetLastError();
+  return launch_kernel(L, kern, tiles, THREADS, sizeof(S), kin, vin, kout, vout, n, shift, dmask, bin_off, desc,
+                       tile_counter, L.status, L.run_if);
 }
 
 template <class K, int THREADS, int KPT, bool HV, bool MATCH>
@@ -625,9 +627,8 @@ static cudaError_t launch_tma(const Launch& L, const K* kin, const uint32_t* vin
   }
   const uint32_t tiles = ceil_div(n, S::TILE);
   const uint32_t grid = min(tiles, (uint32_t)(per_sm * L.num_sms));
-  kern<<<grid, THREADS, sizeof(S), L.stream>>>(kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tile_counter,
-                                               L.status, L.run_if);
-  return cudaGetLastError();
+  return launch_kernel(L, kern, grid, THREADS, sizeof(S), kin, vin, kout, vout, n, shift, dmask, bin_off, desc,
+                       tile_counter, L.status, L.run_if);
 }
 
 template <class K>

@@ -54,16 +54,16 @@ cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d
   if (work == 0 && !d_m) return cudaSuccess;
   if (g_tree_method == 1) {
     const uint32_t u_host = d_u ? 0u : (uint32_t)max(m_host, 0) + 1;
-    if (queue) {
+    if (queue && !L.ws_zeroed) {
       cudaError_t e = cudaMemsetAsync(q_count, 0, 4, L.stream);
       if (e != cudaSuccess) return e;
     }
-    radix_tree_window_kernel<K, false><<<max(1u, ceil_div(work, TW_T)), TW_THREADS, 0, L.stream>>>(
-        codes, d_u, u_host, nullptr, 0, prefix_n, hll, hlr, left, parent, edge, d_m, queue, q_count);
-    if (queue)
-      radix_tree_slow_kernel<K, false><<<L.num_sms * 2, 256, 0, L.stream>>>(
-          codes, d_u, u_host, nullptr, 0, prefix_n, hll, hlr, left, parent, edge, queue, q_count);
-    return cudaGetLastError();
+    cudaError_t e = launch_kernel(L, radix_tree_window_kernel<K, false>, max(1u, ceil_div(work, TW_T)), TW_THREADS, 0,
+                                  codes, d_u, u_host, nullptr, 0u, prefix_n, hll, hlr, left, parent, edge, d_m, queue,
+                                  q_count);
+    if (e != cudaSuccess || !queue) return e;
+    return launch_kernel(L, radix_tree_slow_kernel<K, false>, L.num_sms * 2, 256, 0, codes, d_u, u_host, nullptr, 0u,
+                         prefix_n, hll, hlr, left, parent, edge, queue, q_count);
   }
   const uint32_t grid = max(1u, min(ceil_div(work, TREE_THREADS), (uint32_t)L.num_sms * 8));
   radix_tree_kernel<K><<<grid, TREE_THREADS, 0, L.stream>>>(codes, d_u, m_host, prefix_n, hll, hlr, left, parent,

@@ -289,6 +289,7 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
     uint8_t* __restrict__ prefix_n, uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
     int32_t* __restrict__ left, int32_t* __restrict__ parent, uint32_t* __restrict__ edge, uint32_t* d_m,
     uint32_t* queue, uint32_t* q_count) {
+  griddep_wait();
   constexpr int A = KeyTraits<K>::A;
   __shared__ TwSmem s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -458,6 +459,7 @@ __global__ void __launch_bounds__(256) radix_tree_slow_kernel(const K* __restric
                                                               uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr,
                                                               int32_t* left, int32_t* parent, uint32_t* edge,
                                                               const uint32_t* queue, const uint32_t* q_count) {
+  griddep_wait();
   constexpr int A = KeyTraits<K>::A;
   const uint32_t U = SEG ? uoff[S] : (d_u ? *d_u : u_host);
   const uint32_t nq = *q_count;
