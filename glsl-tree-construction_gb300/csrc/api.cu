@@ -319,7 +319,7 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   {
     StageTimer t(ctx, stream, GTC_STAGE_MORTON);
     // No payload written here: the first sort pass makes the iota itself.
-    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, nullptr, n, mn, rg, Wz,
+    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, n, mn, rg, Wz,
                                        passes));
   }
   bool in_alt = false;  // "alt" here = the caller's keys/idx buffers

@@ -88,6 +88,14 @@ __device__ __forceinline__ uint64_t ld_hint(const uint64_t* p, uint64_t pol) {
   return v;
 }
 
+__device__ __forceinline__ uint4 ld_hint(const uint4* p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+
 __device__ __forceinline__ void st_hint(uint32_t* p, uint32_t v, uint64_t pol) {
   asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
 }
@@ -430,10 +438,11 @@ cudaError_t launch_morton32(const Launch& L, const float4* pts, uint32_t* keys, 
                             float rg);
 cudaError_t launch_morton64(const Launch& L, const float4* pts, uint64_t* keys, uint32_t* idx, uint32_t n, float mn,
                             float rg);
-// Fused Morton encode + iota + global histogram for a following sort.
+// Fused Morton encode + global histogram for a following sort of the full
+// code (passes must be ceil(3B / 8)); zeroes W.desc[0, W.desc_words).
 template <class K>
-cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t* idx, uint32_t n, float mn,
-                               float rg, const SortWorkspace& W, int passes);
+cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t n, float mn, float rg,
+                               const SortWorkspace& W, int passes);
 
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,

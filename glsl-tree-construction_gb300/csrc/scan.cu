@@ -60,18 +60,19 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_scan_kernel(const uint32_t* 
   const uint32_t full_end = beg + ((min(end, limit) > beg ? min(end, limit) - beg : 0u) & ~127u);
   const uint4* in4 = reinterpret_cast<const uint4*>(in);
 
-  // 1. segment totals
+  // 1. segment totals (rows tagged to stay in L2 for step 3)
+  const uint64_t keep_pol = l2_keep_policy(), drop_pol = l2_drop_policy();
   uint32_t sum = 0;
   uint32_t r = beg;
   for (; r + 4 * 128 <= full_end; r += 4 * 128) {
     uint4 v[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = in4[(r + j * 128) / 4 + lane];
+    for (int j = 0; j < 4; ++j) v[j] = ld_hint(in4 + (r + j * 128) / 4 + lane, keep_pol);
 #pragma unroll
     for (int j = 0; j < 4; ++j) sum += v[j].x + v[j].y + v[j].z + v[j].w;
   }
   for (; r < full_end; r += 128) {
-    const uint4 v = in4[r / 4 + lane];
+    const uint4 v = ld_hint(in4 + r / 4 + lane, keep_pol);
     sum += v.x + v.y + v.z + v.w;
   }
   for (uint32_t i = r + lane; i < end; i += 32) sum += (i < limit) ? in[i] : 0u;
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_scan_kernel(const uint32_t* 
     const uint32_t i0 = r + 4 * lane;
     uint4 v;
     if (r + 128 <= full_end) {
-      v = in4[r / 4 + lane];
+      v = ld_hint(in4 + r / 4 + lane, drop_pol);
     } else {
       v.x = (i0 + 0 < end && i0 + 0 < limit) ? in[i0 + 0] : 0u;
       v.y = (i0 + 1 < end && i0 + 1 < limit) ? in[i0 + 1] : 0u;
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __res
   const uint64_t beg64 = (uint64_t)(blockIdx.x * CS_WARPS + warp) * S;
   const uint32_t beg = (uint32_t)min(beg64, (uint64_t)n);
   const uint32_t end = (uint32_t)min(beg64 + S, (uint64_t)n);
-  const uint32_t full_end = beg + ((end - beg) & ~127u);
+  const uint32_t full_end = beg + ((end - beg) & ~255u);
   const K first_prev = (beg > 0 && beg < end) ? kin[beg - 1] : K(0);
 
   // 1. kept keys per segment (keys tagged to stay in L2 for step 3)
@@ -149,12 +150,12 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __res
   {
     K carry = first_prev;
     uint32_t r = beg;
-    for (; r < full_end; r += 128) {
-      K k[4];
+    for (; r < full_end; r += 256) {  // eight rows in flight per warp
+      K k[8];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) k[j] = ld_hint(kin + r + 32 * j + lane, keep_pol);
+      for (int j = 0; j < 8; ++j) k[j] = ld_hint(kin + r + 32 * j + lane, keep_pol);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 8; ++j) {
         K prev = __shfl_up_sync(0xffffffffu, k[j], 1);
         if (lane == 0) prev = carry;
         const bool keep = (r + 32 * j + lane == 0) || k[j] != prev;
@@ -182,16 +183,16 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __res
   {
     K carry = first_prev;
     uint32_t r = beg;
-    for (; r < full_end; r += 128) {
-      K k[4];
-      uint32_t v[4];
+    for (; r < full_end; r += 256) {
+      K k[8];
+      uint32_t v[8];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 8; ++j) {
         k[j] = ld_hint(kin + r + 32 * j + lane, drop_pol);
         if (HAS_VALS) v[j] = ld_hint(vin + r + 32 * j + lane, drop_pol);
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < 8; ++j) {
         K prev = __shfl_up_sync(0xffffffffu, k[j], 1);
         if (lane == 0) prev = carry;
         const bool keep = (r + 32 * j + lane == 0) || k[j] != prev;

@@ -68,8 +68,7 @@ __device__ __forceinline__ void hist_add(uint32_t (*s_hist)[RADIX], K k, int beg
 // the done counter, so the workspace needs no clearing between calls.
 template <int THREADS>
 __device__ __forceinline__ void hist_finish(uint32_t (*s_hist)[RADIX], int passes, uint32_t* counts,
-                                            uint32_t* bin_offsets, uint32_t* done, uint32_t* s_warp_sums,
-                                            uint32_t* s_last) {
+                                            uint32_t* bin_offsets, uint32_t* done, uint32_t* s_last) {
   __syncthreads();
   for (int i = threadIdx.x; i < passes * RADIX; i += THREADS) {
     const uint32_t c = (&s_hist[0][0])[i];
@@ -81,11 +80,35 @@ __device__ __forceinline__ void hist_finish(uint32_t (*s_hist)[RADIX], int passe
   __syncthreads();
   if (*s_last == 0) return;
   __threadfence();
-  for (int p = 0; p < passes; ++p) {
-    const uint32_t c = (threadIdx.x < RADIX) ? __ldcg(&counts[p * RADIX + threadIdx.x]) : 0u;
-    const uint32_t ex = scan256_exclusive<THREADS>(c, s_warp_sums);
-    if (threadIdx.x < RADIX) bin_offsets[p * RADIX + threadIdx.x] = ex;
-    __syncthreads();
+  // The last block turns every pass's counts into offsets at once: one warp
+  // per pass, eight consecutive bins per lane (one round trip for all).
+  static_assert(THREADS / 32 >= MAX_PASSES, "a warp per pass");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < passes) {
+    const uint4* c4 = reinterpret_cast<const uint4*>(counts + warp * RADIX + lane * 8);
+    const uint4 a = __ldcg(c4), b = __ldcg(c4 + 1);
+    uint4 ea, eb;  // lane-local exclusive prefixes
+    ea.x = 0;
+    ea.y = a.x;
+    ea.z = ea.y + a.y;
+    ea.w = ea.z + a.z;
+    eb.x = ea.w + a.w;
+    eb.y = eb.x + b.x;
+    eb.z = eb.y + b.y;
+    eb.w = eb.z + b.z;
+    const uint32_t tot = eb.w + b.w;
+    const uint32_t base = warp_inclusive_sum(tot) - tot;
+    ea.x += base;
+    ea.y += base;
+    ea.z += base;
+    ea.w += base;
+    eb.x += base;
+    eb.y += base;
+    eb.z += base;
+    eb.w += base;
+    uint4* o4 = reinterpret_cast<uint4*>(bin_offsets + warp * RADIX + lane * 8);
+    o4[0] = ea;
+    o4[1] = eb;
   }
   if (threadIdx.x == 0) *done = 0;
 }
@@ -107,7 +130,6 @@ __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restric
                                                               const uint32_t* run_if) {
   if (run_if && *run_if == 0) return;
   __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
-  __shared__ uint32_t s_warp_sums[8];
   __shared__ uint32_t s_last;
   for (int i = threadIdx.x; i < MAX_PASSES * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
   zero_region(zero_ptr, zero_words);
@@ -124,23 +146,36 @@ __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restric
   }
   for (size_t i = (size_t)nvec * VEC + (size_t)blockIdx.x * THREADS + threadIdx.x; i < n; i += stride)
     hist_add<K>(s_hist, keys[i], begin_bit, end_bit, passes);
-  hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, s_warp_sums, &s_last);
+  hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, &s_last);
 }
 
-// Fused Morton encode + iota payload + global histogram: the first stage of
-// the pipeline reads the points once and leaves the sort ready to run.
+// Digit counts of every pass over a full-width Morton code (bits [0, 3B)):
+// the shifts and masks are compile-time constants.
+template <class K>
+__device__ __forceinline__ void hist_add_code(uint32_t (*s_hist)[RADIX], K k) {
+  constexpr int BITS = 3 * KeyTraits<K>::B;
+  constexpr int P = (BITS + 7) / 8;
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    const uint32_t d = (uint32_t)(k >> (8 * p)) & ((1u << (BITS - 8 * p < 8 ? BITS - 8 * p : 8)) - 1u);
+    atomicAdd(&s_hist[p][d], 1u);
+  }
+}
+
+// Fused Morton encode + global histogram of all passes of the following
+// sort over the full code: the first stage of the pipeline reads the points
+// once and leaves the sort ready to run (its first pass makes the index
+// payload itself).
 template <class K, int THREADS, int Q>
-__global__ void __launch_bounds__(THREADS, 2) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
-                                                              uint32_t* __restrict__ idx, uint32_t n, float mn,
-                                                              float rg, float inv_rg, int end_bit, int passes,
-                                                              uint32_t* counts,
-                                                              uint32_t* bin_offsets, uint32_t* done,
+__global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
+                                                              uint32_t n, float mn, float rg, float inv_rg,
+                                                              uint32_t* counts, uint32_t* bin_offsets, uint32_t* done,
                                                               uint32_t* zero_ptr, size_t zero_words) {
   griddep_wait();
-  __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
-  __shared__ uint32_t s_warp_sums[8];
+  constexpr int P = (3 * KeyTraits<K>::B + 7) / 8;
+  __shared__ uint32_t s_hist[P][RADIX];
   __shared__ uint32_t s_last;
-  for (int i = threadIdx.x; i < MAX_PASSES * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < P * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
   zero_region(zero_ptr, zero_words);
   __syncthreads();
   const size_t stride = (size_t)gridDim.x * THREADS;
@@ -153,17 +188,15 @@ __global__ void __launch_bounds__(THREADS, 2) morton_hist_kernel(const float4* _
     for (int u = 0; u < 4; ++u) {
       const K k = encode_point<K, Q>(p[u], mn, rg, inv_rg);
       keys[i + u * stride] = k;
-      if (idx) idx[i + u * stride] = (uint32_t)(i + u * stride);
-      hist_add<K>(s_hist, k, 0, end_bit, passes);
+      hist_add_code<K>(s_hist, k);
     }
   }
   for (; i < n; i += stride) {
     const K k = encode_point<K, Q>(__ldcs(pts + i), mn, rg, inv_rg);
     keys[i] = k;
-    if (idx) idx[i] = (uint32_t)i;
-    hist_add<K>(s_hist, k, 0, end_bit, passes);
+    hist_add_code<K>(s_hist, k);
   }
-  hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, s_warp_sums, &s_last);
+  hist_finish<THREADS>(s_hist, P, counts, bin_offsets, done, &s_last);
 }
 
 // ------------------------------------------------------------ onesweep ----
@@ -716,9 +749,10 @@ template cudaError_t launch_global_hist<uint64_t>(const Launch&, const uint64_t*
                                                   const SortWorkspace&, int);
 
 template <class K>
-cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t* idx, uint32_t n, float mn,
-                               float rg, const SortWorkspace& W, int passes) {
+cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t n, float mn, float rg,
+                               const SortWorkspace& W, int passes) {
   constexpr int T = 512;
+  if (passes != (3 * KeyTraits<K>::B + 7) / 8) return cudaErrorInvalidValue;  // full-width codes only
   const float inv = pow2_reciprocal(rg);
   auto kern = (inv != 0.0f) ? morton_hist_kernel<K, T, 1> : morton_hist_kernel<K, T, 2>;
   // One resident wave: every block loops over the points.
@@ -732,14 +766,13 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
   }
   const uint32_t want = ceil_div(n, T * 8);
   const uint32_t grid = max(1u, min(want, (uint32_t)(L.num_sms * occ)));
-  kern<<<grid, T, 0, L.stream>>>(pts, keys, idx, n, mn, rg, inv, 3 * KeyTraits<K>::B, passes, W.counts,
-                                 W.bin_offsets, W.header, W.desc, W.desc_words);
-  return cudaGetLastError();
+  return launch_kernel(L, kern, grid, T, 0, pts, keys, n, mn, rg, inv, W.counts, W.bin_offsets, W.header, W.desc,
+                       W.desc_words);
 }
-template cudaError_t launch_morton_hist<uint32_t>(const Launch&, const float4*, uint32_t*, uint32_t*, uint32_t, float,
-                                                  float, const SortWorkspace&, int);
-template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, uint64_t*, uint32_t*, uint32_t, float,
-                                                  float, const SortWorkspace&, int);
+template cudaError_t launch_morton_hist<uint32_t>(const Launch&, const float4*, uint32_t*, uint32_t, float, float,
+                                                  const SortWorkspace&, int);
+template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, uint64_t*, uint32_t, float, float,
+                                                  const SortWorkspace&, int);
 
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
