@@ -77,11 +77,17 @@ __device__ __forceinline__ void octree_root_only(gtc_octnode* nodes, uint32_t ca
 // ------------------------------------------- warp batches (pull form) --
 constexpr int OCT_RING = 256;
 
+// A child slot in shared memory: the child's index with a flag for a present
+// child and one for a leaf (indices are < 2^30), so no mask has to be kept
+// beside the slots.
+constexpr uint32_t OCT_PRESENT = 1u << 31, OCT_LEAF = 1u << 30, OCT_INDEX = OCT_LEAF - 1u;
+
 // Per-warp scratch of the make kernel.
 struct OctWarp {
   uint32_t q[64];           // contributing radix nodes waiting for a batch
-  int32_t ch[32][8];        // children of the batch's bottom nodes, by lane
-  uint32_t mk[32];          // child masks found by the descent rounds (node | leaf << 8)
+  uint32_t ch[32][9];       // child slots of the batch's bottom nodes, by lane; rows of 9 words so that
+                            // slot w of different lanes, and different slots of one lane, fall in
+                            // different banks
   uint2 ring[OCT_RING];     // descent candidates {index, owner | leaf << 5 | deep << 6 | level << 8}
 };
 
@@ -97,7 +103,7 @@ struct OctWarp {
 //            descents themselves on valid input (checked).
 // Loads of a candidate's own data (edge, code, offset) and of its children
 // (left, leaf flags) are issued together, so each level costs one round trip.
-// Children and masks collect in shared memory, then every lane writes its
+// Children collect in shared memory as flagged slots, then every lane writes its
 // node (4 x 16 B) and the chain nodes above it.
 // Per-lane cloud of a batch node: codes and tree arrays are indexed
 // globally, the cloud's keys are [u0, mend] (mend = u0 + its radix nodes),
@@ -145,11 +151,8 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
     }
   }
   const int level = dk + 1;
-  int4* chl = reinterpret_cast<int4*>(S.ch[lane]);
-  chl[0] = make_int4(0, 0, 0, 0);
-  chl[1] = make_int4(0, 0, 0, 0);
-  S.mk[lane] = 0;
-  uint32_t nmask = 0, lmask = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) S.ch[lane][w] = 0u;
 
   // Level 1: both radix children of k.
   bool dsc[2] = {false, false};
@@ -161,8 +164,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
     if (ok && leaf) {
       if (WITH_LEAVES) {
         const int w = child_slot<K>(codes[x], level);
-        S.ch[lane][w] = (int32_t)(x - cl.u0);
-        lmask |= 1u << w;
+        S.ch[lane][w] = (x - cl.u0) | OCT_PRESENT | OCT_LEAF;
       }
     } else if (ok) {
       const uint32_t e = edge[x];
@@ -172,8 +174,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
       const uint32_t f = (uint32_t)(hll[x] != 0) | ((uint32_t)(hlr[x] != 0) << 1);
       if (e > 0) {
         const int w = child_slot<K>(cx, level);
-        S.ch[lane][w] = (int32_t)(p - cl.bias);
-        nmask |= 1u << w;
+        S.ch[lane][w] = (p - cl.bias) | OCT_PRESENT;
       } else {
         dsc[side] = true;
         dl[side] = cl.u0 + lx;
@@ -218,8 +219,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
     } else if (have && leaf) {
       if (WITH_LEAVES) {
         const int w = child_slot<K>(codes[y], lev);
-        S.ch[owner][w] = (int32_t)(y - o_u0);
-        atomicOr(&S.mk[owner], 1u << (8 + w));
+        S.ch[owner][w] = (y - o_u0) | OCT_PRESENT | OCT_LEAF;
       }
     } else if (have) {
       const uint32_t e = edge[y];
@@ -231,8 +231,7 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
       }
       if (e > 0) {
         const int w = child_slot<K>(cy, lev);
-        S.ch[owner][w] = (int32_t)(p - o_bias);
-        atomicOr(&S.mk[owner], 1u << w);
+        S.ch[owner][w] = (p - o_bias) | OCT_PRESENT;
       } else if (deep) {
         push = true;
       } else {
@@ -259,10 +258,19 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
   }
 
   if (ok) {
-    const int4 a = chl[0], b = chl[1];
-    const uint32_t mk = S.mk[lane];
-    nmask |= mk & 0xffu;
-    lmask = (lmask | (mk >> 8)) & lmask_keep;
+    uint32_t cv[8], nmask = 0, lmask = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      const uint32_t v = S.ch[lane][w];
+      if (v & OCT_PRESENT) {
+        if (v & OCT_LEAF) lmask |= 1u << w;
+        else nmask |= 1u << w;
+      }
+      cv[w] = v & OCT_INDEX;
+    }
+    lmask &= lmask_keep;
+    const int4 a = make_int4((int)cv[0], (int)cv[1], (int)cv[2], (int)cv[3]);
+    const int4 b = make_int4((int)cv[4], (int)cv[5], (int)cv[6], (int)cv[7]);
     const uint32_t bottom = (kl == 0) ? 0u : top - c + 1;
     // Corners from the cell coordinates decoded once; cell sizes rg / 2^k as
     // the exact scaling rg * 2^-k (octree.comp:111-116, 181-182).
