@@ -54,7 +54,8 @@ def parse_args():
     ap.add_argument("--clouds", type=int, default=512, help="batched workload: number of clouds")
     ap.add_argument("--key-bits", type=int, default=64, help="sort workload: 32 or 64")
     ap.add_argument("--and-words", type=int, default=0, help="sort workload: AND of k uniform words (0 = uniform)")
-    ap.add_argument("--sort-variant", type=int, default=None, help="force a compiled onesweep variant")
+    ap.add_argument("--sort-variant", type=int, default=None,
+                    help="force a compiled onesweep variant (sort and octree workloads; skips the autotuner)")
     return ap.parse_args()
 
 
@@ -216,9 +217,15 @@ def run_gtc(args):
     # Autotune the onesweep shape on this workload's own Morton codes (the
     # pipeline's sort: 63 bits of 64-bit keys); the choice is cached per
     # (key width, bits, ceil(log2 n)) and picked up by the build below.
-    codes, _ = ctx.morton(pts, KEY_BITS, with_idx=False)
-    tune = ctx.autotune_sort(KEY_BITS, n, 0, 63, keys=codes, reps=3)
-    del codes
+    # --sort-variant pins the shape instead (e.g. for a profiler run, where
+    # the serialised launches would distort the autotuner's timings).
+    if args.sort_variant is not None:
+        ctx.set_sort_variant(KEY_BITS, args.sort_variant)
+        tune = {"best": args.sort_variant, "ms": []}
+    else:
+        codes, _ = ctx.morton(pts, KEY_BITS, with_idx=False)
+        tune = ctx.autotune_sort(KEY_BITS, n, 0, 63, keys=codes, reps=3)
+        del codes
     plan = gtc.OctreePlan(ctx, n, KEY_BITS, nodes_capacity=n + (n >> 1))
     for _ in range(max(args.warmup, 3)):
         plan.launch(pts)
@@ -327,7 +334,8 @@ def run_gtc(args):
                    "eager_ms_per_step": round(eager_ms, 4), "stage_ms_per_step": stage_ms,
                    "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
                    "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
-                   "sort_variant": gtc.autotune_lookup(KEY_BITS, 63, n),
+                   "sort_variant": (args.sort_variant if args.sort_variant is not None
+                                    else gtc.autotune_lookup(KEY_BITS, 63, n)),
                    "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
