@@ -293,10 +293,35 @@ def run_gtc(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx.check(L.gtc_build_octree_host(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, hn, cap, cp))
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    L.gtc_host_free(hp)
-    L.gtc_host_free(hn)
+    e2e_sync_s = (time.perf_counter() - t0) / e2e_steps
     assert tuple(int(c) for c in counts) == (u, m, o)
+    # Back-to-back builds through the queued entry point: uploads, node
+    # read-backs and kernels of consecutive builds overlap.  Every step still
+    # moves its own points in and its nodes out; each build in flight has its
+    # own node and count buffers.
+    NQ = 3
+    outs = [hn] + [ctypes.c_void_p() for _ in range(NQ - 1)]
+    hc = [ctypes.c_void_p() for _ in range(NQ)]
+    for h in outs[1:]:
+        ctx.check(L.gtc_host_alloc(ctypes.byref(h), cap * 64))
+    for c in hc:
+        ctx.check(L.gtc_host_alloc(ctypes.byref(c), 16))
+    for i in range(2 * NQ):
+        ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, outs[i % NQ], cap, hc[i % NQ]))
+    ctx.check(L.gtc_build_octree_host_wait(ctx.h))
+    q_steps = max(6, min(args.steps, 30))
+    t0 = time.perf_counter()
+    for i in range(q_steps):
+        ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, outs[i % NQ], cap, hc[i % NQ]))
+    ctx.check(L.gtc_build_octree_host_wait(ctx.h))
+    e2e_s = (time.perf_counter() - t0) / q_steps
+    for c in hc:
+        got = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(c.value))
+        assert tuple(int(x) for x in got) == (u, m, o)
+        L.gtc_host_free(c)
+    L.gtc_host_free(hp)
+    for h in outs:
+        L.gtc_host_free(h)
 
     if rank != 0:
         return
@@ -319,7 +344,7 @@ def run_gtc(args):
     alg_total = sum(alg.values())
     ms_per_step = elapsed_ms / args.steps
     value = world * n / (ms_per_step * 1e-3) / 1e6
-    kernels_per_step = 1 + 8 + 1 + 1 + 1 + 1  # morton+hist, 8 passes, unique, tree, scan, octree
+    kernels_per_step = 1 + 8 + 1 + 2 + 1 + 1  # morton+hist, 8 passes, unique, tree + long splits, scan, octree
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
 
     line = {
@@ -342,7 +367,11 @@ def run_gtc(args):
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "bytes_per_launch": pass_bytes, "avg_launch_ms": round(avg_pass_ms, 5)},
         "e2e": {"value": round(n / e2e_s / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": n * 16,
-                "d2h_bytes_per_step": o * 64 + 16, "api": "gtc_build_octree_host (pinned host buffers)"},
+                "d2h_bytes_per_step": o * 64 + 12,
+                "api": "gtc_build_octree_host_async x steps + gtc_build_octree_host_wait (pinned host buffers, "
+                       "consecutive builds overlapped)",
+                "sync_value": round(n / e2e_sync_s / 1e6, 2),
+                "sync_api": "gtc_build_octree_host, one build at a time"},
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
     }

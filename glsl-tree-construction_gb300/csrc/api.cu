@@ -62,6 +62,21 @@ struct gtc_ctx {
   size_t own_ws_bytes = 0;
   cudaStream_t own_stream = nullptr;
   Resident res;
+  // Queued host builds (gtc_build_octree_host_async): two buffer sets and
+  // streams, used alternately.
+  struct QueuedOut {
+    gtc_octnode* nodes = nullptr;
+    uint32_t cap = 0;
+    uint32_t* counts = nullptr;
+    bool pending = false;  // built, node read-back not yet queued
+  };
+  static constexpr int NQ = 3;  // buffer sets used in turn
+  Resident qres[NQ];
+  cudaStream_t qstream[NQ] = {};  // builds and node read-backs
+  cudaEvent_t qbuilt[NQ] = {};    // the slot's build and its counts are done
+  QueuedOut qout[NQ];
+  gtc_status qerr = GTC_OK;  // first host-side error of a queued build, reported by the wait
+  int qnext = 0;
 };
 
 namespace {
@@ -314,6 +329,8 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   Lp.pdl = !ctx->profiling;
   Lp.ws_zeroed = true;
 
+
+
   GTC_TRY(ctx, cudaMemsetAsync(o->counts, 0, 16, S(stream)));
   GTC_TRY(ctx, cudaMemsetAsync(Wk.header, 0, Wk.header_words * 4, S(stream)));
   {
@@ -367,8 +384,7 @@ void free_resident(Resident& r) {
   r = Resident();
 }
 
-gtc_status ensure_resident(gtc_ctx* ctx, uint32_t n, int key_bits, uint32_t nodes_cap) {
-  Resident& r = ctx->res;
+gtc_status ensure_resident(gtc_ctx* ctx, Resident& r, uint32_t n, int key_bits, uint32_t nodes_cap) {
   if (r.n_cap >= n && r.key_bits == key_bits && r.nodes_cap >= nodes_cap && r.pts) return GTC_OK;
   cudaDeviceSynchronize();
   const uint32_t cap = std::max<uint32_t>(std::max(n, r.key_bits == key_bits ? r.n_cap : 0u), 1);
@@ -466,6 +482,11 @@ GTC_API gtc_status gtc_destroy(gtc_ctx* ctx) {
   }
   for (auto e : ctx->free_events) cudaEventDestroy(e);
   free_resident(ctx->res);
+  for (int q = 0; q < gtc_ctx::NQ; ++q) {
+    free_resident(ctx->qres[q]);
+    if (ctx->qstream[q]) cudaStreamDestroy(ctx->qstream[q]);
+    if (ctx->qbuilt[q]) cudaEventDestroy(ctx->qbuilt[q]);
+  }
   if (ctx->own_ws) cudaFree(ctx->own_ws);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -702,7 +723,7 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
   }
   if (!ctx->own_stream) GTC_TRY(ctx, cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
   cudaStream_t st = ctx->own_stream;
-  gtc_status s = ensure_resident(ctx, n, key_bits, 0);
+  gtc_status s = ensure_resident(ctx, ctx->res, n, key_bits, 0);
   if (s != GTC_OK) return s;
   // Page-locked input is streamed from host memory by the Morton pass itself,
   // so the transfer overlaps the encoding; other host memory is copied first.
@@ -722,7 +743,7 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
     const uint32_t o = c[2];
     if (o > r.nodes_cap) {  // rare: long single-child chains; grow and rebuild
       cudaMemsetAsync(ctx->d_status, 0, 4, st);
-      s = ensure_resident(ctx, n, key_bits, o);
+      s = ensure_resident(ctx, ctx->res, n, key_bits, o);
       if (s != GTC_OK) return s;
       continue;
     }
@@ -735,6 +756,82 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
     return gtc_device_status(ctx, st);
   }
   return fail(ctx, GTC_ERR_CAPACITY, "octree node capacity");
+}
+
+// Queues the node read-back of slot q's finished build on the slot's stream
+// (a copy-engine transfer of exactly o nodes, so it takes no SM time from
+// the build that runs meanwhile).  Waits on the host for that build first.
+static gtc_status queue_readback(gtc_ctx* ctx, int q) {
+  gtc_ctx::QueuedOut& out = ctx->qout[q];
+  if (!out.pending) return GTC_OK;
+  out.pending = false;
+  GTC_TRY(ctx, cudaEventSynchronize(ctx->qbuilt[q]));
+  const uint32_t o = out.counts[2];
+  if (o > ctx->qres[q].nodes_cap) return GTC_OK;  // the build flagged DEV_CAPACITY; the wait reports it
+  if (o > out.cap) {
+    if (ctx->qerr == GTC_OK) ctx->qerr = fail(ctx, GTC_ERR_CAPACITY, "host node buffer too small");
+    return GTC_OK;
+  }
+  if (out.nodes && o)
+    GTC_TRY(ctx, cudaMemcpyAsync(out.nodes, ctx->qres[q].nodes, (size_t)o * sizeof(gtc_octnode),
+                                 cudaMemcpyDeviceToHost, ctx->qstream[q]));
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_build_octree_host_async(gtc_ctx* ctx, const float* host_pts, uint32_t n, float mn, float rg,
+                                               int key_bits, gtc_octnode* host_nodes, uint32_t host_cap,
+                                               uint32_t* host_counts) {
+  GTC_ARG(ctx, ctx, "null context");
+  GTC_ARG(ctx, key_bits == 32 || key_bits == 64, "key_bits must be 32 or 64");
+  GTC_ARG(ctx, n < (1u << 30), "n must be < 2^30");
+  GTC_ARG(ctx, host_counts, "null counts buffer");
+  if (n == 0) {
+    host_counts[0] = host_counts[1] = host_counts[2] = 0;
+    return GTC_OK;
+  }
+  const float* d_in = reinterpret_cast<const float*>(device_view(host_pts));
+  GTC_ARG(ctx, device_view(host_counts), "host_counts must be page-locked");
+  GTC_ARG(ctx, host_pts && d_in && aligned16(d_in), "host_pts must be page-locked and 16-byte aligned");
+  GTC_ARG(ctx, !host_nodes || device_view(host_nodes), "host_nodes must be page-locked");
+  const int q = ctx->qnext;
+  if (!ctx->qstream[q]) {
+    GTC_TRY(ctx, cudaStreamCreateWithFlags(&ctx->qstream[q], cudaStreamNonBlocking));
+    GTC_TRY(ctx, cudaEventCreateWithFlags(&ctx->qbuilt[q], cudaEventDisableTiming));
+  }
+  cudaStream_t st = ctx->qstream[q];
+  // A slot that has to grow synchronises the device first (ensure_resident).
+  gtc_status s = ensure_resident(ctx, ctx->qres[q], n, key_bits, n + (n >> 1) + 1024);
+  if (s != GTC_OK) return s;
+  Resident& r = ctx->qres[q];
+  // The Morton pass reads the page-locked points over the host link itself
+  // (no copy-engine upload, which would queue behind the node read-backs).
+  // The slot's previous node read-back was queued on this stream by a later
+  // call, so stream order keeps the slot's buffers safe.
+  gtc_octree_buffers b{r.keys, r.idx, r.prefix_n, r.hll, r.hlr, r.left, r.parent, r.edge, r.ps, r.nodes,
+                       r.nodes_cap, r.counts};
+  s = gtc_build_octree(ctx, d_in, n, mn, rg, key_bits, &b, r.ws, r.ws_bytes, st);
+  if (s != GTC_OK) return s;
+  GTC_TRY(ctx, cudaMemcpyAsync(host_counts, r.counts, 12, cudaMemcpyDeviceToHost, st));
+  GTC_TRY(ctx, cudaEventRecord(ctx->qbuilt[q], st));
+  ctx->qout[q] = {host_nodes, host_nodes ? host_cap : 0u, host_counts, true};
+  ctx->qnext = (q + 1) % gtc_ctx::NQ;
+  // The previous build is read back while this one runs.
+  return queue_readback(ctx, (q + gtc_ctx::NQ - 1) % gtc_ctx::NQ);
+}
+
+GTC_API gtc_status gtc_build_octree_host_wait(gtc_ctx* ctx) {
+  GTC_ARG(ctx, ctx, "null context");
+  for (int i = 0; i < gtc_ctx::NQ; ++i) {  // oldest slot first
+    const int q = (ctx->qnext + i) % gtc_ctx::NQ;
+    gtc_status s = queue_readback(ctx, q);
+    if (s != GTC_OK) return s;
+  }
+  for (int q = 0; q < gtc_ctx::NQ; ++q)
+    if (ctx->qstream[q]) GTC_TRY(ctx, cudaStreamSynchronize(ctx->qstream[q]));
+  gtc_status s = gtc_device_status(ctx, ctx->qstream[0]);
+  if (s == GTC_OK && ctx->qerr != GTC_OK) s = ctx->qerr;
+  ctx->qerr = GTC_OK;
+  return s;
 }
 
 GTC_API gtc_status gtc_host_alloc(void** ptr, size_t bytes) {

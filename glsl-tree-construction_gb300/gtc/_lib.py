@@ -61,6 +61,8 @@ SIGNATURES = {
     "gtc_link_octree_u64": (st, [P, P, u32, P, P, P, P, P, i32, P, P, P, P]),
     "gtc_build_octree": (st, [P, P, u32, f32, f32, i_, ctypes.POINTER(OctreeBuffers), P, sz, P]),
     "gtc_build_octree_host": (st, [P, P, u32, f32, f32, i_, P, u32, P]),
+    "gtc_build_octree_host_async": (st, [P, P, u32, f32, f32, i_, P, u32, P]),
+    "gtc_build_octree_host_wait": (st, [P]),
     "gtc_host_alloc": (st, [ctypes.POINTER(P), sz]),
     "gtc_host_free": (st, [P]),
     "gtc_sort_pairs_u32_noalloc": (st, [P, P, P, P, P, u32, i_, i_, P]),

@@ -253,6 +253,29 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
                                          float range, int key_bits, gtc_octnode* host_nodes,
                                          uint32_t host_nodes_capacity, uint32_t* host_counts);
 
+/* Queued form of gtc_build_octree_host for back-to-back builds (a stream of
+ * point clouds): the same outputs, with builds overlapped.  Builds take three
+ * sets of device buffers in turn, each with its own streams.  A call queues
+ * its points' upload (a copy engine) and its build, then waits on the host
+ * for the previous build and queues that build's node read-back: a
+ * copy-engine transfer of exactly o nodes.  Uploads, read-backs and kernels
+ * of different builds run at the same time (the host link carries both
+ * directions at once).  host_pts, host_nodes and host_counts must be
+ * page-locked (gtc_host_alloc / cudaHostRegister) and stay untouched until
+ * gtc_build_octree_host_wait returns; builds in flight need distinct output
+ * buffers.  host_counts[0..2] = u, m, o;
+ * host_nodes gets the o nodes (it may be NULL with capacity 0: counts only).
+ * The device node buffer holds 1.5 n + 1024 nodes.  With o above either
+ * capacity the wait returns GTC_ERR_CAPACITY (counts still set, no nodes);
+ * gtc_build_octree_host sizes itself to any o.  n = 0 sets the counts to 0
+ * at once. */
+GTC_API gtc_status gtc_build_octree_host_async(gtc_ctx* ctx, const float* host_pts, uint32_t n, float min_coord,
+                                               float range, int key_bits, gtc_octnode* host_nodes,
+                                               uint32_t host_nodes_capacity, uint32_t* host_counts);
+/* Waits for every queued build of the context; reports the first device
+ * error of any of them (GTC_ERR_CAPACITY, GTC_ERR_TIMEOUT, ...). */
+GTC_API gtc_status gtc_build_octree_host_wait(gtc_ctx* ctx);
+
 /* ---------------------------------------------------- batched clouds ---- */
 /* No counterpart in the reference: many independent point clouds of uneven
  * size built in one stream-ordered sequence of launches (graph-capturable, no

@@ -147,6 +147,50 @@ def test_host_entry_point_pinned_buffers(ctx, oracle):
         L.gtc_host_free(hn)
 
 
+def test_host_entry_point_queued(ctx, oracle):
+    """Three clouds queued back to back through gtc_build_octree_host_async
+    (two device buffer sets in flight, 64- and 32-bit codes), each into its
+    own page-locked buffers: every one equals the oracle.  A node buffer that
+    is too small is reported by the wait, with the counts set, and the
+    context stays usable."""
+    import ctypes
+
+    L = ctx.L
+    jobs = [(W.config2_points(1 << 19, seed=11), 64), (W.config2_points(1 << 19, seed=12), 64),
+            (W.uniform_points(300_001, seed=13), 32)]
+    exps = [oracle.build_octree(p, kb, threads=8)[0] for p, kb in jobs]
+    bufs = []
+    try:
+        for (p, _), e in zip(jobs, exps):
+            hp, hn, hc = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+            ctx.check(L.gtc_host_alloc(ctypes.byref(hp), p.nbytes))
+            ctx.check(L.gtc_host_alloc(ctypes.byref(hn), (e["n_oct_nodes"] + 8) * 64))
+            ctx.check(L.gtc_host_alloc(ctypes.byref(hc), 16))
+            ctypes.memmove(hp, p.ctypes.data, p.nbytes)
+            bufs.append((hp, hn, hc))
+        for (hp, hn, hc), (p, kb), e in zip(bufs, jobs, exps):
+            ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, p.shape[0], 0.0, 1024.0, kb, hn,
+                                                    e["n_oct_nodes"] + 8, hc))
+        ctx.check(L.gtc_build_octree_host_wait(ctx.h))
+        for (hp, hn, hc), e in zip(bufs, exps):
+            c = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(hc.value))
+            o = e["n_oct_nodes"]
+            assert tuple(int(x) for x in c) == (e["n_unique"], e["n_brt_nodes"], o)
+            got = np.ctypeslib.as_array((ctypes.c_int32 * (o * 16)).from_address(hn.value)).reshape(o, 16)
+            assert np.array_equal(got, e["nodes"].view(np.int32).reshape(o, 16))
+        hp, hn, hc = bufs[0]
+        o = exps[0]["n_oct_nodes"]
+        ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, jobs[0][0].shape[0], 0.0, 1024.0, 64, hn, o // 2, hc))
+        assert L.gtc_build_octree_host_wait(ctx.h) == 7  # GTC_ERR_CAPACITY
+        c = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(hc.value))
+        assert int(c[2]) == o
+        ctx.device_status()
+    finally:
+        for b in bufs:
+            for x in b:
+                L.gtc_host_free(x)
+
+
 def test_deterministic_across_runs(ctx):
     import gtc
     import torch
