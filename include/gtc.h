@@ -262,8 +262,9 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
  * of different builds run at the same time (the host link carries both
  * directions at once).  host_pts, host_nodes and host_counts must be
  * page-locked (gtc_host_alloc / cudaHostRegister) and stay untouched until
- * gtc_build_octree_host_wait returns; builds in flight need distinct output
- * buffers.  host_counts[0..2] = u, m, o;
+ * gtc_build_octree_host_wait returns.  Builds in flight need distinct output
+ * buffers, except that every third call may reuse them: calls take the three
+ * buffer sets in turn and a set's writes are ordered on its stream.  host_counts[0..2] = u, m, o;
  * host_nodes gets the o nodes (it may be NULL with capacity 0: counts only).
  * The device node buffer holds 1.5 n + 1024 nodes.  With o above either
  * capacity the wait returns GTC_ERR_CAPACITY (counts still set, no nodes);
