@@ -25,8 +25,11 @@
 //      first chunk holding a smaller value, and one 16-byte SIMD compare
 //      finds the position inside it;
 //   3. a split whose range reaches past the halo (0.04% of the splits of the
-//      10M clustered cloud) is queued for radix_tree_slow_kernel, where a
-//      warp searches the codes cooperatively, 32 probes per round.
+//      10M clustered cloud) is kept in a block-local queue and resolved at
+//      the end of the block by a warp that searches the codes cooperatively,
+//      both range ends together, 32 probes per end per round; splits beyond
+//      the local queue's capacity go to radix_tree_slow_kernel, which does
+//      the same.
 #pragma once
 
 #include "gtc_internal.cuh"
@@ -42,6 +45,7 @@ constexpr int TW_NCH = TW_W / TW_C;        // 640 chunks
 constexpr int TW_NWB = TW_NCH / 32;        // 20 warp-blocks of 32 chunks
 constexpr int TW_TV = 64;                  // prefix lengths are < 64
 constexpr int TW_MAXB = 512;               // cloud starts cached per window (batched)
+constexpr int TW_LQ = 128;                 // long-range splits a block resolves itself
 static_assert(TW_H % (32 * TW_C) == 0, "the tile starts on a warp-block");
 static_assert(TW_NWB <= 32, "one ballot covers the window's warp-blocks");
 
@@ -69,7 +73,8 @@ struct TwSmem {
   uint32_t t4[TW_NWB][TW_TV];    // t4[b][v] bit k: chunk 32b + k has a value < v
   uint32_t t9[TW_TV];            // t9[v] bit b: warp-block b has a value < v
   uint32_t cb[TW_MAXB];          // batched: cloud starts from c_first on
-  uint32_t c_first, nb;
+  uint32_t lq[TW_LQ];            // this block's splits whose range reaches past the window
+  uint32_t c_first, nb, lq_n;
 };
 
 // Bytes of a word below t (prefix lengths < 128): bit 7 of each byte of
@@ -202,31 +207,50 @@ __device__ __forceinline__ int tw_prev_tab(const TwSmem& s, int c, uint32_t t) {
 // with keys further away never increases, so both are monotone searches).
 // Single-thread forms (stage API, no queue) and a warp-cooperative form.
 
-// Largest offset o in [1, lim] with δ(c, code[base + dir * o]) >= t, for a
-// predicate that holds at o = 1 and is monotone: every lane of the warp calls
-// it; each round probes 32 offsets at once (exponentially spaced first, then
-// 32 equal steps of the remaining interval), so a range of 2^20 keys takes
-// 5 dependent rounds instead of 40 probes.
+// Both range ends of split x (prefix length t) in the cloud [first, last]
+// by the whole warp: the largest hi in [x + 1, last] with δ(code_x, code_hi)
+// >= t and the smallest lo in [first, x] with δ(code_{x+1}, code_lo) >= t.
+// Each side is a monotone predicate over an offset o >= 1 that holds at o = 1.
+// Every lane probes one offset of each side per round (the two loads in
+// flight together): exponentially spaced offsets first, then 32 equal steps
+// of each remaining interval, so a range of 2^20 keys takes 5 dependent
+// rounds for both ends.  Every lane of the warp calls it with the same x.
 template <class K>
-__device__ __forceinline__ uint32_t tw_warp_extent(const K* codes, K c, long long base, int dir, uint32_t lim,
-                                                   int t) {
+__device__ __forceinline__ uint2 tw_warp_range(const K* codes, uint32_t x, uint32_t first, uint32_t last, int t) {
   const int lane = threadIdx.x & 31;
-  auto good = [&](uint64_t o) -> bool {
-    return o >= 1 && o <= lim && delta_key(c, codes[base + dir * (long long)o]) >= t;
+  const K cx = codes[x], c1 = codes[x + 1];
+  const uint32_t lim_r = last - x, lim_l = x + 1 - first;  // offsets available on each side
+  auto good_r = [&](uint64_t o) -> bool { return o >= 1 && o <= lim_r && delta_key(cx, codes[x + o]) >= t; };
+  auto good_l = [&](uint64_t o) -> bool {
+    return o >= 1 && o <= lim_l && delta_key(c1, codes[(uint64_t)x + 1 - o]) >= t;
   };
-  const uint32_t eb = __ballot_sync(0xffffffffu, lane < 31 ? good(1ull << lane) : false);
-  const int k = 31 - __clz(eb | 1u);  // o = 1 always holds
-  uint64_t lo_b = 1ull << k;                                            // good
-  uint64_t hi_b = min((uint64_t)(1ull << (k + 1)), (uint64_t)lim + 1);  // first offset known or assumed bad
-  while (hi_b - lo_b > 1) {
-    const uint64_t stride = (hi_b - lo_b + 31) / 32;
-    const uint64_t p = lo_b + (uint64_t)(lane + 1) * stride;
-    const uint32_t b = __ballot_sync(0xffffffffu, p < hi_b && good(p));
-    const uint64_t nlo = b ? lo_b + (uint64_t)(32 - __clz(b)) * stride : lo_b;
-    hi_b = min(nlo + stride, hi_b);
-    lo_b = nlo;
+  bool pr = false, pl = false;
+  if (lane < 31) {
+    pr = good_r(1ull << lane);
+    pl = good_l(1ull << lane);
   }
-  return (uint32_t)lo_b;
+  const uint32_t er = __ballot_sync(0xffffffffu, pr), el = __ballot_sync(0xffffffffu, pl);
+  const int kr = 31 - __clz(er | 1u), kl = 31 - __clz(el | 1u);  // o = 1 always holds
+  uint64_t lo_r = 1ull << kr, hi_r = min((uint64_t)(1ull << (kr + 1)), (uint64_t)lim_r + 1);
+  uint64_t lo_l = 1ull << kl, hi_l = min((uint64_t)(1ull << (kl + 1)), (uint64_t)lim_l + 1);
+  while (hi_r - lo_r > 1 || hi_l - lo_l > 1) {  // warp-uniform
+    const uint64_t sr = (hi_r - lo_r + 31) / 32, sl = (hi_l - lo_l + 31) / 32;
+    const uint64_t qr = lo_r + (uint64_t)(lane + 1) * sr, ql = lo_l + (uint64_t)(lane + 1) * sl;
+    const bool gr = hi_r - lo_r > 1 && qr < hi_r && good_r(qr);
+    const bool gl = hi_l - lo_l > 1 && ql < hi_l && good_l(ql);
+    const uint32_t br = __ballot_sync(0xffffffffu, gr), bl = __ballot_sync(0xffffffffu, gl);
+    if (hi_r - lo_r > 1) {
+      const uint64_t n = br ? lo_r + (uint64_t)(32 - __clz(br)) * sr : lo_r;
+      hi_r = min(n + sr, hi_r);
+      lo_r = n;
+    }
+    if (hi_l - lo_l > 1) {
+      const uint64_t n = bl ? lo_l + (uint64_t)(32 - __clz(bl)) * sl : lo_l;
+      hi_l = min(n + sl, hi_l);
+      lo_l = n;
+    }
+  }
+  return make_uint2(x + 1 - (uint32_t)lo_l, x + (uint32_t)lo_r);
 }
 
 template <class K>
@@ -277,6 +301,23 @@ __device__ __forceinline__ void tw_emit(uint32_t x, uint32_t t, uint32_t lo, uin
   if (hi != x + 1) parent[x + 1] = (int32_t)(idx - U0);
 }
 
+// One split's node found by tw_warp_range (called by a whole warp; lane 0
+// stores), cloud [U0, U1).
+template <class K>
+__device__ __forceinline__ void tw_warp_split(const K* codes, uint32_t x, uint32_t U0, uint32_t U1,
+                                              uint8_t* prefix_n, uint8_t* hll, uint8_t* hlr, int32_t* left,
+                                              int32_t* parent, uint32_t* edge) {
+  constexpr int A = KeyTraits<K>::A;
+  const int t = delta_key(codes[x], codes[x + 1]);
+  const uint2 r = tw_warp_range<K>(codes, x, U0, U1 - 1, t);
+  if ((threadIdx.x & 31) == 0) {
+    const uint32_t lo = r.x, hi = r.y;
+    const uint32_t dR = (hi + 1 < U1) ? (uint32_t)delta_key(codes[hi], codes[hi + 1]) : 0u;
+    const uint32_t dL = (lo > U0) ? (uint32_t)delta_key(codes[lo - 1], codes[lo]) : 0u;
+    tw_emit<A>(x, (uint32_t)t, lo, hi, dL, dR, U0, prefix_n, hll, hlr, left, parent, edge);
+  }
+}
+
 // One block: splits [blockIdx.x * T, + T).  SEG: clouds of codes start at
 // uoff[0..S] (uoff[S] = U), indices written are cloud-local, and the last
 // slot of every cloud gets edge 0.  Otherwise one cloud of U codes.  With a
@@ -284,7 +325,7 @@ __device__ __forceinline__ void tw_emit(uint32_t x, uint32_t t, uint32_t lo, uin
 // the halo are appended to it for radix_tree_slow_kernel; without one they
 // are searched here by their own thread.
 template <class K, bool SEG>
-__global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
+__global__ void __launch_bounds__(TW_THREADS, 4) radix_tree_window_kernel(
     const K* __restrict__ codes, const uint32_t* d_u, uint32_t u_host, const uint32_t* uoff, uint32_t S,
     uint8_t* __restrict__ prefix_n, uint8_t* __restrict__ hll, uint8_t* __restrict__ hlr,
     int32_t* __restrict__ left, int32_t* __restrict__ parent, uint32_t* __restrict__ edge, uint32_t* d_m,
@@ -301,6 +342,7 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
   const int x_end = min(t0 + TW_T, (int)(SEG ? U : P));
   if (t0 >= x_end) return;
   const int w0 = t0 - TW_H;
+  if (tid == 0) s.lq_n = 0;
 
   // 1. prefix lengths of the window's pairs.
   // Four adjacent pairs per thread and step: five codes (two 16-byte loads
@@ -426,9 +468,16 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
     }
     const int r = (lr & 15) ? cstart + (int)(lr & 15) : tw_next_tab(s, chunk, t);
     const int l = (lr >> 4) != 15 ? cstart + (int)(lr >> 4) : tw_prev_tab(s, chunk, t);
-    if ((r < 0 || l < 0) && queue) {
-      queue[atomicAdd(q_count, 1u)] = x;
-      continue;
+    if (r < 0 || l < 0) {  // the range reaches past the window: step 5, or the queue
+      const uint32_t k = atomicAdd(&s.lq_n, 1u);
+      if (k < (uint32_t)TW_LQ) {
+        s.lq[k] = x;
+        continue;
+      }
+      if (queue) {
+        queue[atomicAdd(q_count, 1u)] = x;
+        continue;
+      }
     }
     uint32_t hi, dR;
     if (r >= 0) {
@@ -448,6 +497,21 @@ __global__ void __launch_bounds__(TW_THREADS) radix_tree_window_kernel(
     }
     tw_emit<A>(x, t, lo, hi, dL, dR, U0, prefix_n, hll, hlr, left, parent, edge);
   }
+
+  // 5. the block's long-range splits, one warp each (both ends searched
+  // over the codes together).
+  __syncthreads();
+  const uint32_t nl = min(s.lq_n, (uint32_t)TW_LQ);
+  for (uint32_t q = warp; q < nl; q += TW_THREADS / 32) {  // warp-uniform
+    const uint32_t x = s.lq[q];
+    uint32_t U0 = 0, U1 = U;
+    if (SEG) {
+      const uint32_t c = owner(uoff, S, x);
+      U0 = uoff[c];
+      U1 = uoff[c + 1];
+    }
+    tw_warp_split<K>(codes, x, U0, U1, prefix_n, hll, hlr, left, parent, edge);
+  }
 }
 
 // The queued splits, one warp each: both range ends by warp-cooperative
@@ -460,10 +524,8 @@ __global__ void __launch_bounds__(256) radix_tree_slow_kernel(const K* __restric
                                                               int32_t* left, int32_t* parent, uint32_t* edge,
                                                               const uint32_t* queue, const uint32_t* q_count) {
   griddep_wait();
-  constexpr int A = KeyTraits<K>::A;
   const uint32_t U = SEG ? uoff[S] : (d_u ? *d_u : u_host);
   const uint32_t nq = *q_count;
-  const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x / 32);
   for (uint32_t q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); q < nq; q += warps) {
     const uint32_t x = queue[q];
@@ -473,15 +535,7 @@ __global__ void __launch_bounds__(256) radix_tree_slow_kernel(const K* __restric
       U0 = uoff[c];
       U1 = uoff[c + 1];
     }
-    const K cx = codes[x], c1 = codes[x + 1];
-    const int t = delta_key(cx, c1);
-    const uint32_t hi = x + tw_warp_extent<K>(codes, cx, x, 1, U1 - 1 - x, t);
-    const uint32_t lo = x + 1 - tw_warp_extent<K>(codes, c1, (long long)x + 1, -1, x + 1 - U0, t);
-    if (lane == 0) {
-      const uint32_t dR = (hi + 1 < U1) ? (uint32_t)delta_key(codes[hi], codes[hi + 1]) : 0u;
-      const uint32_t dL = (lo > U0) ? (uint32_t)delta_key(codes[lo - 1], codes[lo]) : 0u;
-      tw_emit<A>(x, (uint32_t)t, lo, hi, dL, dR, U0, prefix_n, hll, hlr, left, parent, edge);
-    }
+    tw_warp_split<K>(codes, x, U0, U1, prefix_n, hll, hlr, left, parent, edge);
   }
 }
 
