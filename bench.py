@@ -36,6 +36,7 @@ N_POINTS = 10_000_000
 LEARNED_KEYS = 64 << 20
 KEY_BITS = 64
 WORKLOAD = "octree_clustered_10M_u64"
+SORT_BEGIN_BIT = 16  # the pipeline's 64-bit sort: onesweep passes over bits 16..62, then the run fixup
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -127,12 +128,16 @@ class ClockSampler:
 # ------------------------------------------------------ algorithmic bytes --
 def algorithmic_bytes(n, u, m, o, K=8):
     """Compulsory bytes of each stage reading its inputs once and writing its
-    outputs once (per-stage figures of the reference's stage surface)."""
-    P = 8 if K == 8 else 4
+    outputs once (per-stage figures of the reference's stage surface).  The
+    sort counts the passes the pipeline runs: 64-bit codes take 6 passes over
+    bits 16..62 plus one read of the keys by the run fixup; 32-bit codes take
+    4 passes."""
+    P = 6 if K == 8 else 4
     return {
         "morton": 16 * n + (K + 4) * n,
         "histogram": K * n,
         "onesweep": P * 2 * (K + 4) * n,
+        "run_fixup": (K * n) if K == 8 else 0,
         "unique": (K + 4) * n + (K + 4) * u,
         "radix_tree": K * u + 11 * m,
         "edge_count": 10 * m,
@@ -224,7 +229,7 @@ def run_gtc(args):
         tune = {"best": args.sort_variant, "ms": []}
     else:
         codes, _ = ctx.morton(pts, KEY_BITS, with_idx=False)
-        tune = ctx.autotune_sort(KEY_BITS, n, 0, 63, keys=codes, reps=3)
+        tune = ctx.autotune_sort(KEY_BITS, n, SORT_BEGIN_BIT, 63, keys=codes, reps=3)
         del codes
     plan = gtc.OctreePlan(ctx, n, KEY_BITS, nodes_capacity=n + (n >> 1))
     for _ in range(max(args.warmup, 3)):
@@ -344,7 +349,7 @@ def run_gtc(args):
     alg_total = sum(alg.values())
     ms_per_step = elapsed_ms / args.steps
     value = world * n / (ms_per_step * 1e-3) / 1e6
-    kernels_per_step = 1 + 8 + 1 + 2 + 1 + 1  # morton+hist, 8 passes, unique, tree + long splits, scan, octree
+    kernels_per_step = 1 + 6 + 1 + 1 + 2 + 1 + 1  # morton+hist, 6 passes, run fixup, unique, tree + long splits, scan, octree
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
 
     line = {
@@ -352,7 +357,7 @@ def run_gtc(args):
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
-                   "onesweep_passes": 8, "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
+                   "onesweep_passes": 6, "sort_bits": "16..62, then the run fixup over bits 0..15", "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
                    "n_oct_nodes": o, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (160 MB of points, ~1 GB working set per build)",
                    "timing": "CUDA-graph replay of the whole build per step",
@@ -360,7 +365,7 @@ def run_gtc(args):
                    "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
                    "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
                    "sort_variant": (args.sort_variant if args.sort_variant is not None
-                                    else gtc.autotune_lookup(KEY_BITS, 63, n)),
+                                    else gtc.autotune_lookup(KEY_BITS, 63 - SORT_BEGIN_BIT, n)),
                    "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

@@ -167,9 +167,17 @@ gtc_status resolve_ws(gtc_ctx* ctx, void*& ws, size_t ws_bytes, size_t need) {
   return GTC_OK;
 }
 
+// The fused pipeline sorts 64-bit codes by onesweep passes over bits
+// [RUN_FIXUP_BITS, 63) and completes the order with the run fixup; 32-bit
+// codes take every pass.
+template <class K>
+constexpr int pipeline_begin_bit() {
+  return sizeof(K) == 8 ? RUN_FIXUP_BITS : 0;
+}
+
 template <class K>
 size_t pipeline_ws_bytes(uint32_t n) {
-  const int passes = passes_for(0, 3 * KeyTraits<K>::B);
+  const int passes = passes_for(pipeline_begin_bit<K>(), 3 * KeyTraits<K>::B);
   size_t b = align_up((size_t)n * sizeof(K), 256);   // keys_alt
   b += align_up((size_t)n * 4, 256);                  // vals_alt
   b += sort_workspace_bytes(n, passes, 0);
@@ -299,7 +307,8 @@ template <class K>
 gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float rg, const gtc_octree_buffers* o,
                     void* ws, size_t ws_bytes, gtc_stream_t stream) {
   constexpr int B = KeyTraits<K>::B;
-  const int passes = passes_for(0, 3 * B);
+  constexpr int BEGIN = pipeline_begin_bit<K>();
+  const int passes = passes_for(BEGIN, 3 * B);
   gtc_status st = resolve_ws(ctx, ws, ws_bytes, pipeline_ws_bytes<K>(n));
   if (st != GTC_OK) return st;
   const Launch L = launch_of(ctx, stream);
@@ -336,7 +345,7 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   {
     StageTimer t(ctx, stream, GTC_STAGE_MORTON);
     // No payload written here: the first sort pass makes the iota itself.
-    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, n, mn, rg, Wz,
+    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, n, mn, rg, Wz, BEGIN,
                                        passes));
   }
   bool in_alt = false;  // "alt" here = the caller's keys/idx buffers
@@ -344,9 +353,18 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
     std::vector<cudaEvent_t> ev;
     if (ctx->profiling)
       for (int i = 0; i < 2 * passes; ++i) ev.push_back(get_event(ctx));
-    GTC_TRY(ctx, launch_onesweep_passes<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, 0, 3 * B, Wk, passes, &in_alt,
-                                           ev.empty() ? nullptr : ev.data(), -1, true));
+    GTC_TRY(ctx, launch_onesweep_passes<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN, 3 * B, Wk, passes,
+                                           &in_alt, ev.empty() ? nullptr : ev.data(), -1, true));
     for (int p = 0; p < (int)ev.size() / 2; ++p) ctx->pending.push_back({ev[2 * p], ev[2 * p + 1], GTC_STAGE_ONESWEEP});
+  }
+  if (BEGIN) {
+    // The low bits decide only within runs of equal high bits: sort those
+    // runs in place; the other pair of buffers is free as scratch.
+    StageTimer t(ctx, stream, GTC_STAGE_RUN_FIXUP);
+    if (in_alt)
+      GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys, o->idx, keys_alt, vals_alt, n, BEGIN));
+    else
+      GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_UNIQUE);

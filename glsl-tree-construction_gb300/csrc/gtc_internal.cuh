@@ -438,11 +438,22 @@ cudaError_t launch_morton32(const Launch& L, const float4* pts, uint32_t* keys, 
                             float rg);
 cudaError_t launch_morton64(const Launch& L, const float4* pts, uint64_t* keys, uint32_t* idx, uint32_t n, float mn,
                             float rg);
-// Fused Morton encode + global histogram for a following sort of the full
-// code (passes must be ceil(3B / 8)); zeroes W.desc[0, W.desc_words).
+// Low bits of a 64-bit Morton code that the pipeline's sort leaves to the
+// run fixup: its onesweep passes cover bits [RUN_FIXUP_BITS, 63).
+constexpr int RUN_FIXUP_BITS = 16;
+// Fused Morton encode + global histogram for a following sort of bits
+// [begin_bit, 3B) of the code (begin_bit 0 or RUN_FIXUP_BITS; passes must be
+// ceil((3B - begin_bit) / 8)); zeroes W.desc[0, W.desc_words).
 template <class K>
 cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t n, float mn, float rg,
-                               const SortWorkspace& W, int passes);
+                               const SortWorkspace& W, int begin_bit, int passes);
+// Completes a stable LSD sort over bits [low_bits, 64) into a sort of the
+// whole key: every run of keys that agree above low_bits is sorted stably by
+// its low bits (1 <= low_bits <= 16), in place; the scratch arrays hold n
+// entries.
+template <class K>
+cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
+                             uint32_t n, int low_bits);
 
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,

@@ -149,30 +149,31 @@ __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restric
   hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, &s_last);
 }
 
-// Digit counts of every pass over a full-width Morton code (bits [0, 3B)):
-// the shifts and masks are compile-time constants.
-template <class K>
+// Digit counts of every pass over bits [LB, 3B) of a Morton code: the
+// shifts and masks are compile-time constants.
+template <class K, int LB>
 __device__ __forceinline__ void hist_add_code(uint32_t (*s_hist)[RADIX], K k) {
   constexpr int BITS = 3 * KeyTraits<K>::B;
-  constexpr int P = (BITS + 7) / 8;
+  constexpr int P = (BITS - LB + 7) / 8;
 #pragma unroll
   for (int p = 0; p < P; ++p) {
-    const uint32_t d = (uint32_t)(k >> (8 * p)) & ((1u << (BITS - 8 * p < 8 ? BITS - 8 * p : 8)) - 1u);
+    const int sh = LB + 8 * p;
+    const uint32_t d = (uint32_t)(k >> sh) & ((1u << (BITS - sh < 8 ? BITS - sh : 8)) - 1u);
     atomicAdd(&s_hist[p][d], 1u);
   }
 }
 
 // Fused Morton encode + global histogram of all passes of the following
-// sort over the full code: the first stage of the pipeline reads the points
-// once and leaves the sort ready to run (its first pass makes the index
-// payload itself).
-template <class K, int THREADS, int Q>
+// sort over bits [LB, 3B) of the code: the first stage of the pipeline reads
+// the points once and leaves the sort ready to run (its first pass makes
+// the index payload itself).
+template <class K, int THREADS, int Q, int LB>
 __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* __restrict__ pts, K* __restrict__ keys,
                                                               uint32_t n, float mn, float rg, float inv_rg,
                                                               uint32_t* counts, uint32_t* bin_offsets, uint32_t* done,
                                                               uint32_t* zero_ptr, size_t zero_words) {
   griddep_wait();
-  constexpr int P = (3 * KeyTraits<K>::B + 7) / 8;
+  constexpr int P = (3 * KeyTraits<K>::B - LB + 7) / 8;
   __shared__ uint32_t s_hist[P][RADIX];
   __shared__ uint32_t s_last;
   for (int i = threadIdx.x; i < P * RADIX; i += THREADS) (&s_hist[0][0])[i] = 0;
@@ -188,16 +189,252 @@ __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* _
     for (int u = 0; u < 4; ++u) {
       const K k = encode_point<K, Q>(p[u], mn, rg, inv_rg);
       keys[i + u * stride] = k;
-      hist_add_code<K>(s_hist, k);
+      hist_add_code<K, LB>(s_hist, k);
     }
   }
   for (; i < n; i += stride) {
     const K k = encode_point<K, Q>(__ldcs(pts + i), mn, rg, inv_rg);
     keys[i] = k;
-    hist_add_code<K>(s_hist, k);
+    hist_add_code<K, LB>(s_hist, k);
   }
   hist_finish<THREADS>(s_hist, P, counts, bin_offsets, done, &s_last);
 }
+
+// --------------------------------------------------------- run fixup ----
+// A stable LSD sort over bits [lb, 64) only leaves keys that agree above bit
+// lb together, in their original order.  Sorting every such run stably by
+// its low lb bits completes the sort of the whole key: the low digits decide
+// only among keys whose high digits tie.  For point-cloud Morton codes these
+// runs are rare and short (13,923 of the 10M clustered codes for lb = 16, at
+// most 5 long), so two 8-bit passes over every key become one read of the
+// keys.  Each warp scans a tile of rows and takes the runs that start in it:
+// up to 32 elements are ranked in registers; longer runs are sorted by two
+// stable 8-bit counting passes through the scratch arrays (any length, one
+// warp, linear time).  Runs whose low bits are already in order are left
+// as they are.
+constexpr int FX_THREADS = 256;
+constexpr int FX_TILE = 32 * 32;  // keys per warp tile
+constexpr int FX_ROWS = 8;        // rows of 32 keys loaded together
+
+template <class K>
+__device__ __forceinline__ bool fx_same(K a, K b, int lb) {
+  return (a >> lb) == (b >> lb);
+}
+
+// Run starting at s, by one lane: if it holds at most FX_LANE keys, sorts it
+// in registers (odd-even transposition over FX_LANE slots; swapping only on
+// strictly greater low bits keeps it stable) and returns true; longer runs
+// are left to the whole warp.  Many short runs of a tile proceed at once.
+constexpr int FX_LANE = 8;
+template <class K>
+__device__ __forceinline__ bool fx_lane_run(K* keys, uint32_t* vals, uint32_t s, uint32_t n, int lb) {
+  const K lmask = (K(1) << lb) - 1;
+  K kk[FX_LANE + 1];
+#pragma unroll
+  for (int q = 0; q <= FX_LANE; ++q) kk[q] = (s + q < n) ? keys[s + q] : K(0);
+  uint32_t g = 1;
+#pragma unroll
+  for (int q = 1; q <= FX_LANE; ++q)
+    if (g == (uint32_t)q && s + q < n && fx_same(kk[q], kk[0], lb)) g = q + 1;
+  if (g > (uint32_t)FX_LANE) return false;
+  bool sorted = true;
+#pragma unroll
+  for (int q = 1; q < FX_LANE; ++q)
+    if ((uint32_t)q < g && (kk[q - 1] & lmask) > (kk[q] & lmask)) sorted = false;
+  if (sorted) return true;
+  uint32_t vv[FX_LANE];
+#pragma unroll
+  for (int q = 0; q < FX_LANE; ++q) vv[q] = (uint32_t)q < g ? vals[s + q] : 0u;
+#pragma unroll
+  for (int round = 0; round < FX_LANE; ++round) {
+#pragma unroll
+    for (int q = round & 1; q + 1 < FX_LANE; q += 2) {
+      if ((uint32_t)(q + 1) < g && (kk[q] & lmask) > (kk[q + 1] & lmask)) {
+        const K tk = kk[q];
+        kk[q] = kk[q + 1];
+        kk[q + 1] = tk;
+        const uint32_t tv = vv[q];
+        vv[q] = vv[q + 1];
+        vv[q + 1] = tv;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < FX_LANE; ++q)
+    if ((uint32_t)q < g) {
+      keys[s + q] = kk[q];
+      vals[s + q] = vv[q];
+    }
+  return true;
+}
+
+// Run [s, s + g), 2 <= g <= 32, ranked by (low bits, position) in registers.
+template <class K>
+__device__ __forceinline__ void fx_short_run(K* keys, uint32_t* vals, uint32_t s, uint32_t g, int lb) {
+  const int lane = threadIdx.x & 31;
+  const bool in = (uint32_t)lane < g;
+  const K k = in ? keys[s + lane] : K(0);
+  const uint32_t v = in ? vals[s + lane] : 0u;
+  const uint32_t lo = (uint32_t)(k & ((K(1) << lb) - 1));
+  const uint32_t pl = __shfl_up_sync(0xffffffffu, lo, 1);
+  if (__ballot_sync(0xffffffffu, in && lane > 0 && pl > lo) == 0) return;  // already in order
+  uint32_t rank = 0;
+  for (uint32_t i = 0; i < g; ++i) {  // warp-uniform
+    const uint32_t li = __shfl_sync(0xffffffffu, lo, (int)i);
+    rank += (li < lo || (li == lo && i < (uint32_t)lane)) ? 1u : 0u;
+  }
+  __syncwarp();
+  if (in) {
+    keys[s + rank] = k;
+    vals[s + rank] = v;
+  }
+}
+
+// Run [s, s + g), g > 32: two stable counting passes over the low bits
+// (bits 0-7, then 8-15), through the scratch arrays and back.  cnt is this
+// warp's 256 shared counters.
+template <class K>
+__device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32_t s, uint32_t g, int lb,
+                            uint32_t* cnt) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  const K lmask = (K(1) << lb) - 1;
+  bool bad = false;
+  for (uint32_t i = 1 + lane; i < g; i += 32) bad |= (keys[s + i - 1] & lmask) > (keys[s + i] & lmask);
+  if (__ballot_sync(0xffffffffu, bad) == 0) return;  // already in order (runs of equal keys)
+  for (int pass = 0; pass < 2; ++pass) {
+    const K* ik = pass ? sk : keys;
+    const uint32_t* iv = pass ? sv : vals;
+    K* ok = pass ? keys : sk;
+    uint32_t* ov = pass ? vals : sv;
+    const int sh = 8 * pass;
+    for (int b = lane; b < 256; b += 32) cnt[b] = 0;
+    __syncwarp();
+    for (uint32_t i = lane; i < g; i += 32) atomicAdd(&cnt[(uint32_t)(ik[s + i] >> sh) & 255u], 1u);
+    __syncwarp();
+    uint32_t c[8], tot = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      c[j] = cnt[lane * 8 + j];
+      tot += c[j];
+    }
+    uint32_t base = warp_inclusive_sum(tot) - tot;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      cnt[lane * 8 + j] = base;
+      base += c[j];
+    }
+    __syncwarp();
+    for (uint32_t r0 = 0; r0 < g; r0 += 32) {  // rounds of 32 in order: stable
+      const uint32_t i = r0 + lane;
+      const bool in = i < g;
+      const K k = in ? ik[s + i] : K(0);
+      const uint32_t v = in ? iv[s + i] : 0u;
+      const uint32_t d = in ? ((uint32_t)(k >> sh) & 255u) : 256u + (uint32_t)lane;  // idle lanes: own digit
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t pos = in ? cnt[d] + __popc(peers & lt) : 0u;
+      __syncwarp();
+      if (in && (peers >> lane) == 1u) cnt[d] += __popc(peers);  // the highest peer advances the digit
+      __syncwarp();
+      if (in) {
+        ok[s + pos] = k;
+        ov[s + pos] = v;
+      }
+    }
+    __syncwarp();  // the pass's writes are visible to the warp's next reads
+  }
+}
+
+template <class K>
+__global__ void __launch_bounds__(FX_THREADS) run_fixup_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
+                                                              uint32_t n, int lb) {
+  griddep_wait();
+  __shared__ uint32_t s_cnt[FX_THREADS / 32][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t gw = blockIdx.x * (FX_THREADS / 32) + warp, nw = gridDim.x * (FX_THREADS / 32);
+  for (uint32_t t0 = gw * FX_TILE; t0 < n; t0 += nw * FX_TILE) {  // warp-uniform
+    const uint32_t t1 = min(t0 + (uint32_t)FX_TILE, n);
+    for (uint32_t r0 = t0; r0 < t1; r0 += FX_ROWS * 32) {
+      // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
+      // lb (a second, offset load, mostly served by L1); one ballot per row.
+      // A run fixed below may permute keys of later rows already loaded
+      // here; all keys of a run share their high bits, so nothing changes.
+      K kr[FX_ROWS], kn[FX_ROWS];
+#pragma unroll
+      for (int j = 0; j < FX_ROWS; ++j) {
+        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+        const bool ok = i < t1 && i + 1 < n;
+        kr[j] = ok ? keys[i] : K(0);
+        kn[j] = ok ? keys[i + 1] : K(0);
+      }
+      // Does the run through r0 start before r0 (owned by another tile)?
+      bool carry = false;
+      if (r0 > 0) carry = fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
+      uint32_t mine = 0, rows = 0;  // lane j keeps row j's run starts; bit j: row j has some
+#pragma unroll
+      for (int j = 0; j < FX_ROWS; ++j) {
+        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+        const uint32_t dup = __ballot_sync(0xffffffffu, i < t1 && i + 1 < n && fx_same(kr[j], kn[j], lb));
+        const uint32_t starts = dup & ~((dup << 1) | (carry ? 1u : 0u));
+        carry = (dup >> 31) != 0;
+        if (lane == j) mine = starts;
+        if (starts) rows |= 1u << j;
+      }
+      if (!rows) continue;  // warp-uniform: runs are rare
+      // Each lane sorts the short runs that start at its position in any of
+      // the rows, all lanes at once; the warp then takes the longer ones.
+      uint32_t mycols = 0;  // bit j: a run starts at this lane's position of row j
+#pragma unroll
+      for (int j = 0; j < FX_ROWS; ++j)
+        if ((__shfl_sync(0xffffffffu, mine, j) >> lane) & 1u) mycols |= 1u << j;
+      uint32_t longer = 0;
+      while (mycols) {  // per lane
+        const int j = __ffs(mycols) - 1;
+        mycols &= mycols - 1;
+        if (!fx_lane_run<K>(keys, vals, r0 + (uint32_t)j * 32 + lane, n, lb)) longer |= 1u << j;
+      }
+      __syncwarp();  // the lanes' writes are visible to the warp
+      if (!__any_sync(0xffffffffu, longer != 0)) continue;
+#pragma unroll 1
+      for (int j = 0; j < FX_ROWS; ++j) {
+        uint32_t bal = __ballot_sync(0xffffffffu, (longer >> j) & 1u);
+        while (bal) {
+          const uint32_t s = r0 + (uint32_t)j * 32 + (uint32_t)(__ffs(bal) - 1);
+          bal &= bal - 1;
+          const K ks = keys[s];  // any key of the run: they share the high bits
+          uint32_t g = 0;        // run length: first key past s + 1 that differs above lb
+          for (uint32_t e = s + 2;; e += 32) {
+            const uint32_t q = e + lane;
+            const bool differs = q >= n || !fx_same(keys[q], ks, lb);
+            const uint32_t bq = __ballot_sync(0xffffffffu, differs);
+            if (bq) {
+              g = e + (uint32_t)(__ffs(bq) - 1) - s;
+              break;
+            }
+          }
+          if (g <= 32) fx_short_run<K>(keys, vals, s, g, lb);
+          else fx_long_run<K>(keys, vals, sk, sv, s, g, lb, s_cnt[warp]);
+        }
+      }
+    }
+  }
+}
+
+template <class K>
+cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
+                             uint32_t n, int low_bits) {
+  if (n < 2) return cudaSuccess;
+  if (low_bits < 1 || low_bits > 16) return cudaErrorInvalidValue;  // two 8-bit passes at most
+  const uint32_t tiles = ceil_div(n, (uint32_t)FX_TILE);
+  const uint32_t grid = max(1u, min(ceil_div(tiles, FX_THREADS / 32), (uint32_t)L.num_sms * 8));
+  return launch_kernel(L, run_fixup_kernel<K>, grid, FX_THREADS, 0, keys, vals, scratch_keys, scratch_vals, n,
+                       low_bits);
+}
+template cudaError_t launch_run_fixup<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t,
+                                                int);
+template cudaError_t launch_run_fixup<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*, uint32_t,
+                                                int);
 
 // ------------------------------------------------------------ onesweep ----
 template <class K, int THREADS, int KPT>
@@ -750,14 +987,20 @@ template cudaError_t launch_global_hist<uint64_t>(const Launch&, const uint64_t*
 
 template <class K>
 cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t n, float mn, float rg,
-                               const SortWorkspace& W, int passes) {
+                               const SortWorkspace& W, int begin_bit, int passes) {
   constexpr int T = 512;
-  if (passes != (3 * KeyTraits<K>::B + 7) / 8) return cudaErrorInvalidValue;  // full-width codes only
+  constexpr int BITS = 3 * KeyTraits<K>::B;
+  if ((begin_bit != 0 && begin_bit != RUN_FIXUP_BITS) || passes != (BITS - begin_bit + 7) / 8)
+    return cudaErrorInvalidValue;  // the code from bit 0, or from the run-fixup boundary
   const float inv = pow2_reciprocal(rg);
-  auto kern = (inv != 0.0f) ? morton_hist_kernel<K, T, 1> : morton_hist_kernel<K, T, 2>;
+  const int form = (inv != 0.0f ? 0 : 1) + (begin_bit ? 2 : 0);
+  auto kern = form == 0 ? morton_hist_kernel<K, T, 1, 0>
+            : form == 1 ? morton_hist_kernel<K, T, 2, 0>
+            : form == 2 ? morton_hist_kernel<K, T, 1, RUN_FIXUP_BITS>
+                        : morton_hist_kernel<K, T, 2, RUN_FIXUP_BITS>;
   // One resident wave: every block loops over the points.
-  static int resident[2] = {0, 0};  // blocks per SM of each form, queried once
-  int& occ = resident[inv != 0.0f ? 0 : 1];
+  static int resident[4] = {0, 0, 0, 0};  // blocks per SM of each form, queried once
+  int& occ = resident[form];
   if (occ == 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, T, 0) != cudaSuccess || occ < 1) {
       cudaGetLastError();
@@ -770,9 +1013,9 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
                        W.desc_words);
 }
 template cudaError_t launch_morton_hist<uint32_t>(const Launch&, const float4*, uint32_t*, uint32_t, float, float,
-                                                  const SortWorkspace&, int);
+                                                  const SortWorkspace&, int, int);
 template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, uint64_t*, uint32_t, float, float,
-                                                  const SortWorkspace&, int);
+                                                  const SortWorkspace&, int, int);
 
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,

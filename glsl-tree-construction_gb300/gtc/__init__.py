@@ -19,7 +19,7 @@ from ._lib import OctreeBuffers
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "OVERFLOW_FALLBACK",
           6: "UNSUPPORTED", 7: "CAPACITY"}
 OP_SORT_PAIRS, OP_UNIQUE, OP_PARTIAL_SUM, OP_BUILD_OCTREE, OP_GLOBAL_HISTOGRAM = 1, 2, 3, 4, 5
-STAGES = ("morton", "histogram", "onesweep", "unique", "radix_tree", "prefix_sum", "octree", "learned")
+STAGES = ("morton", "histogram", "onesweep", "unique", "radix_tree", "prefix_sum", "octree", "learned", "run_fixup")
 
 OCTNODE_DTYPE = np.dtype([("children", "<i4", (8,)), ("corner", "<f4", (4,)), ("cell_size", "<f4"),
                           ("child_node_mask", "<i4"), ("child_leaf_mask", "<i4"), ("_pad", "<i4")])
@@ -96,10 +96,10 @@ class Context:
         self.check(self.L.gtc_set_profiling(self.h, 1 if on else 0))
 
     def stage_times(self, reset: bool = True) -> dict:
-        ms = (ctypes.c_float * 8)()
-        n = (ctypes.c_uint32 * 8)()
+        ms = (ctypes.c_float * len(STAGES))()
+        n = (ctypes.c_uint32 * len(STAGES))()
         self.check(self.L.gtc_stage_times(self.h, ms, n, 1 if reset else 0))
-        return {STAGES[i]: (ms[i], n[i]) for i in range(8)}
+        return {STAGES[i]: (ms[i], n[i]) for i in range(len(STAGES))}
 
     def workspace_size(self, op: int, n: int, key_bits: int) -> int:
         b = ctypes.c_size_t()

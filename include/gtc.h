@@ -80,7 +80,8 @@ GTC_API const char* gtc_version(void);
 /* Record per-stage CUDA events around every launch (0 = off, the default). */
 GTC_API gtc_status gtc_set_profiling(gtc_ctx* ctx, int enable);
 /* Sum of event-timed milliseconds per stage since the last reset, and the
- * number of launches timed.  Stages: see GTC_STAGE_*.  Synchronises. */
+ * number of launches timed; ms and launches hold GTC_STAGE_COUNT entries.
+ * Stages: see GTC_STAGE_*.  Synchronises. */
 enum {
   GTC_STAGE_MORTON = 0,
   GTC_STAGE_HISTOGRAM = 1,
@@ -90,7 +91,8 @@ enum {
   GTC_STAGE_PREFIX_SUM = 5,
   GTC_STAGE_OCTREE = 6,
   GTC_STAGE_LEARNED = 7,
-  GTC_STAGE_COUNT = 8
+  GTC_STAGE_RUN_FIXUP = 8, /* the fused pipeline's low-bit fixup after its 64-bit sort */
+  GTC_STAGE_COUNT = 9
 };
 GTC_API gtc_status gtc_stage_times(gtc_ctx* ctx, float* ms, uint32_t* launches, int reset);
 
