@@ -213,7 +213,6 @@ __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* _
 // warp, linear time).  Runs whose low bits are already in order are left
 // as they are.
 constexpr int FX_THREADS = 256;
-constexpr int FX_TILE = 32 * 32;  // keys per warp tile
 constexpr int FX_ROWS = 8;        // rows of 32 keys loaded together
 
 template <class K>
@@ -346,95 +345,96 @@ __device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32
   }
 }
 
+// Finds the runs: every position where a run of two or more keys starts is
+// appended to list (warp-aggregated; the order does not matter).
 template <class K>
-__global__ void __launch_bounds__(FX_THREADS) run_fixup_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
-                                                              uint32_t n, int lb) {
+__global__ void __launch_bounds__(FX_THREADS) run_detect_kernel(const K* __restrict__ keys, uint32_t n, int lb,
+                                                               uint32_t* __restrict__ list, uint32_t* list_count) {
+  griddep_wait();
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = blockIdx.x * (FX_THREADS / 32) + (threadIdx.x >> 5), nw = gridDim.x * (FX_THREADS / 32);
+  for (uint32_t r0 = gw * FX_ROWS * 32; r0 < n; r0 += nw * FX_ROWS * 32) {  // warp-uniform
+    // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
+    // lb (a second, offset load, mostly served by L1); one ballot per row.
+    K kr[FX_ROWS], kn[FX_ROWS];
+#pragma unroll
+    for (int j = 0; j < FX_ROWS; ++j) {
+      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+      const bool ok = i + 1 < n;
+      kr[j] = ok ? keys[i] : K(0);
+      kn[j] = ok ? keys[i + 1] : K(0);
+    }
+    // Does the run through r0 start before it?
+    bool carry = r0 > 0 && fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
+#pragma unroll
+    for (int j = 0; j < FX_ROWS; ++j) {
+      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+      const uint32_t dup = __ballot_sync(0xffffffffu, i + 1 < n && fx_same(kr[j], kn[j], lb));
+      const uint32_t starts = dup & ~((dup << 1) | (carry ? 1u : 0u));
+      carry = (dup >> 31) != 0;
+      if (starts) {  // warp-uniform
+        uint32_t at = 0;
+        if (lane == 0) at = atomicAdd(list_count, (uint32_t)__popc(starts));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if ((starts >> lane) & 1u) list[at + __popc(starts & ((1u << lane) - 1u))] = i;
+      }
+    }
+  }
+}
+
+// Sorts the listed runs: each lane the short run at one list entry, then the
+// warp the longer runs its lanes met, one by one.
+template <class K>
+__global__ void __launch_bounds__(FX_THREADS) run_sort_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
+                                                             uint32_t n, int lb, const uint32_t* __restrict__ list,
+                                                             const uint32_t* list_count) {
   griddep_wait();
   __shared__ uint32_t s_cnt[FX_THREADS / 32][256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t gw = blockIdx.x * (FX_THREADS / 32) + warp, nw = gridDim.x * (FX_THREADS / 32);
-  for (uint32_t t0 = gw * FX_TILE; t0 < n; t0 += nw * FX_TILE) {  // warp-uniform
-    const uint32_t t1 = min(t0 + (uint32_t)FX_TILE, n);
-    for (uint32_t r0 = t0; r0 < t1; r0 += FX_ROWS * 32) {
-      // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
-      // lb (a second, offset load, mostly served by L1); one ballot per row.
-      // A run fixed below may permute keys of later rows already loaded
-      // here; all keys of a run share their high bits, so nothing changes.
-      K kr[FX_ROWS], kn[FX_ROWS];
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j) {
-        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-        const bool ok = i < t1 && i + 1 < n;
-        kr[j] = ok ? keys[i] : K(0);
-        kn[j] = ok ? keys[i + 1] : K(0);
-      }
-      // Does the run through r0 start before r0 (owned by another tile)?
-      bool carry = false;
-      if (r0 > 0) carry = fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
-      uint32_t mine = 0, rows = 0;  // lane j keeps row j's run starts; bit j: row j has some
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j) {
-        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-        const uint32_t dup = __ballot_sync(0xffffffffu, i < t1 && i + 1 < n && fx_same(kr[j], kn[j], lb));
-        const uint32_t starts = dup & ~((dup << 1) | (carry ? 1u : 0u));
-        carry = (dup >> 31) != 0;
-        if (lane == j) mine = starts;
-        if (starts) rows |= 1u << j;
-      }
-      if (!rows) continue;  // warp-uniform: runs are rare
-      // Each lane sorts the short runs that start at its position in any of
-      // the rows, all lanes at once; the warp then takes the longer ones.
-      uint32_t mycols = 0;  // bit j: a run starts at this lane's position of row j
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j)
-        if ((__shfl_sync(0xffffffffu, mine, j) >> lane) & 1u) mycols |= 1u << j;
-      uint32_t longer = 0;
-      while (mycols) {  // per lane
-        const int j = __ffs(mycols) - 1;
-        mycols &= mycols - 1;
-        if (!fx_lane_run<K>(keys, vals, r0 + (uint32_t)j * 32 + lane, n, lb)) longer |= 1u << j;
-      }
-      __syncwarp();  // the lanes' writes are visible to the warp
-      if (!__any_sync(0xffffffffu, longer != 0)) continue;
-#pragma unroll 1
-      for (int j = 0; j < FX_ROWS; ++j) {
-        uint32_t bal = __ballot_sync(0xffffffffu, (longer >> j) & 1u);
-        while (bal) {
-          const uint32_t s = r0 + (uint32_t)j * 32 + (uint32_t)(__ffs(bal) - 1);
-          bal &= bal - 1;
-          const K ks = keys[s];  // any key of the run: they share the high bits
-          uint32_t g = 0;        // run length: first key past s + 1 that differs above lb
-          for (uint32_t e = s + 2;; e += 32) {
-            const uint32_t q = e + lane;
-            const bool differs = q >= n || !fx_same(keys[q], ks, lb);
-            const uint32_t bq = __ballot_sync(0xffffffffu, differs);
-            if (bq) {
-              g = e + (uint32_t)(__ffs(bq) - 1) - s;
-              break;
-            }
-          }
-          if (g <= 32) fx_short_run<K>(keys, vals, s, g, lb);
-          else fx_long_run<K>(keys, vals, sk, sv, s, g, lb, s_cnt[warp]);
+  const uint32_t cnt = *list_count;
+  for (uint32_t base = gw * 32; base < cnt; base += nw * 32) {  // warp-uniform
+    const uint32_t e = base + lane;
+    const uint32_t s0 = e < cnt ? list[e] : 0u;
+    const bool longer = e < cnt && !fx_lane_run<K>(keys, vals, s0, n, lb);
+    __syncwarp();  // the lanes' writes are visible to the warp
+    uint32_t bal = __ballot_sync(0xffffffffu, longer);
+    while (bal) {  // warp-uniform
+      const uint32_t s = __shfl_sync(0xffffffffu, s0, __ffs(bal) - 1);
+      bal &= bal - 1;
+      const K ks = keys[s];  // any key of the run: they share the high bits
+      uint32_t g = 0;        // run length: first key past s + 1 that differs above lb
+      for (uint32_t q0 = s + 2;; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        const bool differs = q >= n || !fx_same(keys[q], ks, lb);
+        const uint32_t bq = __ballot_sync(0xffffffffu, differs);
+        if (bq) {
+          g = q0 + (uint32_t)(__ffs(bq) - 1) - s;
+          break;
         }
       }
+      if (g <= 32) fx_short_run<K>(keys, vals, s, g, lb);
+      else fx_long_run<K>(keys, vals, sk, sv, s, g, lb, s_cnt[warp]);
     }
   }
 }
 
 template <class K>
 cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
-                             uint32_t n, int low_bits) {
+                             uint32_t n, int low_bits, uint32_t* list, uint32_t* list_count) {
   if (n < 2) return cudaSuccess;
   if (low_bits < 1 || low_bits > 16) return cudaErrorInvalidValue;  // two 8-bit passes at most
-  const uint32_t tiles = ceil_div(n, (uint32_t)FX_TILE);
-  const uint32_t grid = max(1u, min(ceil_div(tiles, FX_THREADS / 32), (uint32_t)L.num_sms * 8));
-  return launch_kernel(L, run_fixup_kernel<K>, grid, FX_THREADS, 0, keys, vals, scratch_keys, scratch_vals, n,
-                       low_bits);
+  const uint32_t rows = ceil_div(n, (uint32_t)(FX_ROWS * 32));
+  const uint32_t grid = max(1u, min(ceil_div(rows, FX_THREADS / 32), (uint32_t)L.num_sms * 8));
+  cudaError_t e = launch_kernel(L, run_detect_kernel<K>, grid, FX_THREADS, 0, keys, n, low_bits, list, list_count);
+  if (e != cudaSuccess) return e;
+  return launch_kernel(L, run_sort_kernel<K>, (uint32_t)L.num_sms * 4, FX_THREADS, 0, keys, vals, scratch_keys,
+                       scratch_vals, n, low_bits, list, list_count);
 }
 template cudaError_t launch_run_fixup<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t,
-                                                int);
+                                                int, uint32_t*, uint32_t*);
 template cudaError_t launch_run_fixup<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*, uint32_t,
-                                                int);
+                                                int, uint32_t*, uint32_t*);
 
 // ------------------------------------------------------------ onesweep ----
 template <class K, int THREADS, int KPT>
