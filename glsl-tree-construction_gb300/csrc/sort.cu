@@ -207,11 +207,12 @@ __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* _
 // only among keys whose high digits tie.  For point-cloud Morton codes these
 // runs are rare and short (13,923 of the 10M clustered codes for lb = 16, at
 // most 5 long), so two 8-bit passes over every key become one read of the
-// keys.  Each warp scans a tile of rows and takes the runs that start in it:
-// up to 32 elements are ranked in registers; longer runs are sorted by two
-// stable 8-bit counting passes through the scratch arrays (any length, one
-// warp, linear time).  Runs whose low bits are already in order are left
-// as they are.
+// keys.  run_detect_kernel streams the keys and lists every run start;
+// run_sort_kernel takes the list: a run of up to FX_LANE keys is sorted by
+// one lane (all lanes at once), up to 32 are ranked in registers by a warp,
+// and longer runs are sorted by two stable 8-bit counting passes through the
+// scratch arrays (any length, one warp, linear time).  Runs whose low bits
+// are already in order are left as they are.
 constexpr int FX_THREADS = 256;
 constexpr int FX_ROWS = 8;        // rows of 32 keys loaded together
 
@@ -223,7 +224,7 @@ __device__ __forceinline__ bool fx_same(K a, K b, int lb) {
 // Run starting at s, by one lane: if it holds at most FX_LANE keys, sorts it
 // in registers (odd-even transposition over FX_LANE slots; swapping only on
 // strictly greater low bits keeps it stable) and returns true; longer runs
-// are left to the whole warp.  Many short runs of a tile proceed at once.
+// are left to the whole warp.
 constexpr int FX_LANE = 8;
 template <class K>
 __device__ __forceinline__ bool fx_lane_run(K* keys, uint32_t* vals, uint32_t s, uint32_t n, int lb) {
