@@ -788,11 +788,12 @@ static gtc_status queue_readback(gtc_ctx* ctx, int q) {
   GTC_TRY(ctx, cudaEventSynchronize(ctx->qbuilt[q]));
   const uint32_t o = out.counts[2];
   if (o > ctx->qres[q].nodes_cap) return GTC_OK;  // the build flagged DEV_CAPACITY; the wait reports it
+  if (!out.nodes) return GTC_OK;                   // counts only
   if (o > out.cap) {
     if (ctx->qerr == GTC_OK) ctx->qerr = fail(ctx, GTC_ERR_CAPACITY, "host node buffer too small");
     return GTC_OK;
   }
-  if (out.nodes && o)
+  if (o)
     GTC_TRY(ctx, cudaMemcpyAsync(out.nodes, ctx->qres[q].nodes, (size_t)o * sizeof(gtc_octnode),
                                  cudaMemcpyDeviceToHost, ctx->qstream[q]));
   return GTC_OK;

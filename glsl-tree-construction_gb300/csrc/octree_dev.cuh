@@ -88,7 +88,8 @@ struct OctWarp {
   uint32_t ch[32][9];       // child slots of the batch's bottom nodes, by lane; rows of 9 words so that
                             // slot w of different lanes, and different slots of one lane, fall in
                             // different banks
-  uint2 ring[OCT_RING];     // descent candidates {index, owner | leaf << 5 | deep << 6 | level << 8}
+  alignas(16) uint2 ring[OCT_RING];  // descent candidates {index, owner | leaf << 5 | deep << 6 | level << 8};
+                                     // pushed in pairs at even positions, one 16-byte store per pair
 };
 
 // One batch of up to 32 contributing radix nodes, one per lane (k valid when
@@ -191,8 +192,8 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
 #pragma unroll
     for (int side = 0; side < 2; ++side) {
       if (dsc[side]) {
-        S.ring[pos] = make_uint2(dl[side], meta | ((df[side] & 1u) << 5));
-        S.ring[pos + 1] = make_uint2(dl[side] + 1, meta | ((df[side] >> 1) << 5));
+        *reinterpret_cast<uint4*>(&S.ring[pos]) =
+            make_uint4(dl[side], meta | ((df[side] & 1u) << 5), dl[side] + 1, meta | ((df[side] >> 1) << 5));
         pos += 2;
       }
     }
@@ -250,8 +251,8 @@ __device__ __forceinline__ void octree_warp_batch(OctWarp& S, bool valid, uint32
     if (push) {
       const uint32_t pos = tail + 2u * __popc(bp & lt);
       const uint32_t meta = owner | ((uint32_t)lev << 8);
-      S.ring[pos % OCT_RING] = make_uint2(ly, meta | ((fy & 1u) << 5));
-      S.ring[(pos + 1) % OCT_RING] = make_uint2(ly + 1, meta | ((fy >> 1) << 5));
+      *reinterpret_cast<uint4*>(&S.ring[pos % OCT_RING]) =  // pos is even: the pair does not wrap
+          make_uint4(ly, meta | ((fy & 1u) << 5), ly + 1, meta | ((fy >> 1) << 5));
     }
     tail += npush;
     __syncwarp();

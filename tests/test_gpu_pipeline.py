@@ -204,6 +204,17 @@ def test_host_entry_point_queued(ctx, oracle):
         c = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(hc.value))
         assert int(c[2]) == o
         ctx.device_status()
+        # Pageable buffers are refused (GTC_ERR_INVALID_ARG) before anything is queued; counts only
+        # (no node buffer) and n = 0 are accepted.
+        pageable = np.ascontiguousarray(jobs[0][0])
+        assert L.gtc_build_octree_host_async(ctx.h, pageable.ctypes.data_as(ctypes.c_void_p), pageable.shape[0],
+                                             0.0, 1024.0, 64, hn, o + 8, hc) == 1
+        ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, jobs[0][0].shape[0], 0.0, 1024.0, 64, None, 0, hc))
+        ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, 0, 0.0, 1024.0, 64, hn, o + 8, bufs[1][2]))
+        ctx.check(L.gtc_build_octree_host_wait(ctx.h))
+        assert tuple(int(x) for x in c) == (exps[0]["n_unique"], exps[0]["n_brt_nodes"], o)
+        c1 = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(bufs[1][2].value))
+        assert tuple(int(x) for x in c1) == (0, 0, 0)
     finally:
         for b in bufs:
             for x in b:
