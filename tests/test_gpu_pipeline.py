@@ -80,6 +80,8 @@ def test_edge_cases(ctx, oracle, key_bits):
         "n1": p([[1.0, 2.0, 3.0]]),
         "n2": p([[1.0, 2.0, 3.0], [700.0, 2.0, 3.0]]),
         "all_equal": p([[5.5, 6.5, 7.5]] * 5000),
+        # one run of a million equal codes: the run fixup's long path finds it in order
+        "all_equal_1m": p(np.tile([[5.5, 6.5, 7.5]], (1 << 20, 1))),
         "corners": p([[x, y, z] for z in (10.0, 600.0) for y in (10.0, 600.0) for x in (10.0, 600.0)]),
         "boundary": p([[1024.0, 0.0, 0.0], [0.0, 1023.99, 0.0], [0.0, 0.0, 0.0], [512.0, 512.0, 512.0]]),
         "duplicates": np.repeat(W.uniform_points(3000, seed=4), 7, axis=0),
