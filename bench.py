@@ -3,8 +3,9 @@
 
 Workload (default): 10,000,000 points from a 32-component isotropic Gaussian
 mixture (sigma 0.5% of the domain, 2% uniform noise), 64-bit Morton codes at
-21 bits per axis, 8 onesweep passes carrying u32 point indices, unique, Karras
-radix tree + edge count, node offsets, octree make+link.  One step = one full
+21 bits per axis, 5 onesweep passes over bits 23..62 carrying u32 point
+indices and a run fixup over the low 23 bits (the same order as 8 passes),
+unique, Karras radix tree + edge count, node offsets, octree make+link.  One step = one full
 build of that cloud.  Metric: Mpoints/s of the full build.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gtc|reference]
@@ -36,7 +37,7 @@ N_POINTS = 10_000_000
 LEARNED_KEYS = 64 << 20
 KEY_BITS = 64
 WORKLOAD = "octree_clustered_10M_u64"
-SORT_BEGIN_BIT = 16  # the pipeline's 64-bit sort: onesweep passes over bits 16..62, then the run fixup
+SORT_BEGIN_BIT = 23  # the pipeline's 64-bit sort: onesweep passes over bits 23..62, then the run fixup
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -129,10 +130,10 @@ class ClockSampler:
 def algorithmic_bytes(n, u, m, o, K=8):
     """Compulsory bytes of each stage reading its inputs once and writing its
     outputs once (per-stage figures of the reference's stage surface).  The
-    sort counts the passes the pipeline runs: 64-bit codes take 6 passes over
-    bits 16..62 plus one read of the keys by the run fixup; 32-bit codes take
+    sort counts the passes the pipeline runs: 64-bit codes take 5 passes over
+    bits 23..62 plus one read of the keys by the run fixup; 32-bit codes take
     4 passes."""
-    P = 6 if K == 8 else 4
+    P = 5 if K == 8 else 4
     return {
         "morton": 16 * n + (K + 4) * n,
         "histogram": K * n,
@@ -349,7 +350,7 @@ def run_gtc(args):
     alg_total = sum(alg.values())
     ms_per_step = elapsed_ms / args.steps
     value = world * n / (ms_per_step * 1e-3) / 1e6
-    kernels_per_step = 1 + 6 + 2 + 1 + 2 + 1 + 1  # morton+hist, 6 passes, run detect + sort, unique, tree + long splits, scan, octree
+    kernels_per_step = 1 + 5 + 2 + 1 + 2 + 1 + 1  # morton+hist, 5 passes, run detect + sort, unique, tree + long splits, scan, octree
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
 
     line = {
@@ -357,7 +358,7 @@ def run_gtc(args):
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
-                   "onesweep_passes": 6, "sort_bits": "16..62, then the run fixup over bits 0..15", "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
+                   "onesweep_passes": 5, "sort_bits": "23..62, then the run fixup over bits 0..22", "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
                    "n_oct_nodes": o, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (160 MB of points, ~1 GB working set per build)",
                    "timing": "CUDA-graph replay of the whole build per step",

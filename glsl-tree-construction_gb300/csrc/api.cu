@@ -344,36 +344,38 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
 
   GTC_TRY(ctx, cudaMemsetAsync(o->counts, 0, 16, S(stream)));
   GTC_TRY(ctx, cudaMemsetAsync(Wk.header, 0, Wk.header_words * 4, S(stream)));
+  // The codes start in whichever pair of buffers makes the last sort pass
+  // write the workspace pair (keys_alt, vals_alt): unique then compacts out
+  // of place into the caller's buffers, which lets it use its resident
+  // segment form.
+  const bool odd_passes = (passes & 1) != 0;
+  K* k0 = odd_passes ? keys : keys_alt;
+  uint32_t* v0 = odd_passes ? o->idx : vals_alt;
+  K* k1 = odd_passes ? keys_alt : keys;
+  uint32_t* v1 = odd_passes ? vals_alt : o->idx;
   {
     StageTimer t(ctx, stream, GTC_STAGE_MORTON);
     // No payload written here: the first sort pass makes the iota itself.
-    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), keys_alt, n, mn, rg, Wz, BEGIN,
-                                       passes));
+    GTC_TRY(ctx, launch_morton_hist<K>(L, reinterpret_cast<const float4*>(pts), k0, n, mn, rg, Wz, BEGIN, passes));
   }
-  bool in_alt = false;  // "alt" here = the caller's keys/idx buffers
   {
+    bool in_second = false;  // true for odd pass counts: then k1 holds the result, else k0
     std::vector<cudaEvent_t> ev;
     if (ctx->profiling)
       for (int i = 0; i < 2 * passes; ++i) ev.push_back(get_event(ctx));
-    GTC_TRY(ctx, launch_onesweep_passes<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN, 3 * B, Wk, passes,
-                                           &in_alt, ev.empty() ? nullptr : ev.data(), -1, true));
+    GTC_TRY(ctx, launch_onesweep_passes<K>(Lp, k0, v0, k1, v1, n, BEGIN, 3 * B, Wk, passes, &in_second,
+                                           ev.empty() ? nullptr : ev.data(), -1, true));
     for (int p = 0; p < (int)ev.size() / 2; ++p) ctx->pending.push_back({ev[2 * p], ev[2 * p + 1], GTC_STAGE_ONESWEEP});
   }
   if (BEGIN) {
     // The low bits decide only within runs of equal high bits: sort those
-    // runs in place; the other pair of buffers is free as scratch.
+    // runs in place; the caller's pair of buffers is free as scratch.
     StageTimer t(ctx, stream, GTC_STAGE_RUN_FIXUP);
-    if (in_alt)
-      GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys, o->idx, keys_alt, vals_alt, n, BEGIN, run_list, q_count + 1));
-    else
-      GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN, run_list, q_count + 1));
+    GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN, run_list, q_count + 1));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_UNIQUE);
-    if (in_alt)  // sorted data already in the caller's buffers: in place
-      GTC_TRY(ctx, launch_unique<K>(Lp, keys, o->idx, keys, o->idx, n, o->counts + 0, unique_ws));
-    else
-      GTC_TRY(ctx, launch_unique<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, o->counts + 0, unique_ws));
+    GTC_TRY(ctx, launch_unique<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, o->counts + 0, unique_ws));
   }
   {
     // vals_alt is free once unique has compacted: it holds the queue of

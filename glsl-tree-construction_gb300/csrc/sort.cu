@@ -205,14 +205,15 @@ __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* _
 // lb together, in their original order.  Sorting every such run stably by
 // its low lb bits completes the sort of the whole key: the low digits decide
 // only among keys whose high digits tie.  For point-cloud Morton codes these
-// runs are rare and short (13,923 of the 10M clustered codes for lb = 16, at
-// most 5 long), so two 8-bit passes over every key become one read of the
-// keys.  run_detect_kernel streams the keys and lists every run start;
-// run_sort_kernel takes the list: a run of up to FX_LANE keys is sorted by
-// one lane (all lanes at once), up to 32 are ranked in registers by a warp,
-// and longer runs are sorted by two stable 8-bit counting passes through the
-// scratch arrays (any length, one warp, linear time).  Runs whose low bits
-// are already in order are left as they are.
+// runs are short (277,486 runs of 2 to 20 keys in the 10M clustered codes
+// for lb = 23, 0.66M keys in all), so three 8-bit passes over every key
+// become one read of the keys and a few touches of 7% of them.  run_detect_kernel
+// streams the keys and lists every run start; run_sort_kernel takes the
+// list: a run of up to FX_LANE keys is sorted by one lane (all lanes at
+// once), up to 32 are ranked in registers by a warp, and longer runs are
+// sorted by stable 8-bit counting passes through the scratch arrays (any
+// length, one warp, linear time).  Runs whose low bits are already in order
+// are left as they are.
 constexpr int FX_THREADS = 256;
 constexpr int FX_ROWS = 8;        // rows of 32 keys loaded together
 
@@ -268,16 +269,16 @@ __device__ __forceinline__ bool fx_lane_run(K* keys, uint32_t* vals, uint32_t s,
   return true;
 }
 
-// Run [s, s + g), 2 <= g <= 32, ranked by (low bits, position) in registers.
+// Run [s, s + g), 2 <= g <= 32, ranked by (low bits, position) in registers;
+// lane l holds key s + l (loaded by the caller).
 template <class K>
-__device__ __forceinline__ void fx_short_run(K* keys, uint32_t* vals, uint32_t s, uint32_t g, int lb) {
+__device__ __forceinline__ void fx_short_run(K* keys, uint32_t* vals, uint32_t s, uint32_t g, int lb, K k) {
   const int lane = threadIdx.x & 31;
   const bool in = (uint32_t)lane < g;
-  const K k = in ? keys[s + lane] : K(0);
-  const uint32_t v = in ? vals[s + lane] : 0u;
   const uint32_t lo = (uint32_t)(k & ((K(1) << lb) - 1));
   const uint32_t pl = __shfl_up_sync(0xffffffffu, lo, 1);
   if (__ballot_sync(0xffffffffu, in && lane > 0 && pl > lo) == 0) return;  // already in order
+  const uint32_t v = in ? vals[s + lane] : 0u;
   uint32_t rank = 0;
   for (uint32_t i = 0; i < g; ++i) {  // warp-uniform
     const uint32_t li = __shfl_sync(0xffffffffu, lo, (int)i);
@@ -290,8 +291,10 @@ __device__ __forceinline__ void fx_short_run(K* keys, uint32_t* vals, uint32_t s
   }
 }
 
-// Run [s, s + g), g > 32: two stable counting passes over the low bits
-// (bits 0-7, then 8-15), through the scratch arrays and back.  cnt is this
+// Run [s, s + g), g >= 32: stable counting passes over the low bits, 8 at a
+// time from bit 0, alternating between the keys and the scratch arrays (an
+// odd number of passes ends with a copy back).  Digits that reach above lb
+// hold bits the whole run shares, so they order nothing.  cnt is this
 // warp's 256 shared counters.
 template <class K>
 __device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32_t s, uint32_t g, int lb,
@@ -302,11 +305,13 @@ __device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32
   bool bad = false;
   for (uint32_t i = 1 + lane; i < g; i += 32) bad |= (keys[s + i - 1] & lmask) > (keys[s + i] & lmask);
   if (__ballot_sync(0xffffffffu, bad) == 0) return;  // already in order (runs of equal keys)
-  for (int pass = 0; pass < 2; ++pass) {
-    const K* ik = pass ? sk : keys;
-    const uint32_t* iv = pass ? sv : vals;
-    K* ok = pass ? keys : sk;
-    uint32_t* ov = pass ? vals : sv;
+  const int npass = (lb + 7) / 8;
+  for (int pass = 0; pass < npass; ++pass) {
+    const bool odd = pass & 1;
+    const K* ik = odd ? sk : keys;
+    const uint32_t* iv = odd ? sv : vals;
+    K* ok = odd ? keys : sk;
+    uint32_t* ov = odd ? vals : sv;
     const int sh = 8 * pass;
     for (int b = lane; b < 256; b += 32) cnt[b] = 0;
     __syncwarp();
@@ -344,49 +349,86 @@ __device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32
     }
     __syncwarp();  // the pass's writes are visible to the warp's next reads
   }
+  if (npass & 1) {  // the last pass wrote the scratch arrays
+    for (uint32_t i = lane; i < g; i += 32) {
+      keys[s + i] = sk[s + i];
+      vals[s + i] = sv[s + i];
+    }
+    __syncwarp();
+  }
 }
 
 // Finds the runs: every position where a run of two or more keys starts is
-// appended to list (warp-aggregated; the order does not matter).
+// appended to list (the order does not matter).  Each block takes 2,048
+// consecutive keys at a time and reserves its entries with one atomic: the
+// 10M clustered codes hold about one start per 20 keys, too many for a
+// counter taken per warp.
 template <class K>
 __global__ void __launch_bounds__(FX_THREADS) run_detect_kernel(const K* __restrict__ keys, uint32_t n, int lb,
                                                                uint32_t* __restrict__ list, uint32_t* list_count) {
   griddep_wait();
-  const int lane = threadIdx.x & 31;
-  const uint32_t gw = blockIdx.x * (FX_THREADS / 32) + (threadIdx.x >> 5), nw = gridDim.x * (FX_THREADS / 32);
-  for (uint32_t r0 = gw * FX_ROWS * 32; r0 < n; r0 += nw * FX_ROWS * 32) {  // warp-uniform
-    // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
-    // lb (a second, offset load, mostly served by L1); one ballot per row.
-    K kr[FX_ROWS], kn[FX_ROWS];
+  constexpr int WARPS = FX_THREADS / 32;
+  constexpr uint32_t BLOCK_KEYS = WARPS * FX_ROWS * 32;
+  __shared__ uint32_t s_off[WARPS];
+  __shared__ uint32_t s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint32_t b0 = blockIdx.x * BLOCK_KEYS; b0 < n; b0 += gridDim.x * BLOCK_KEYS) {  // block-uniform
+    const uint32_t r0 = b0 + (uint32_t)warp * FX_ROWS * 32;
+    uint32_t st[FX_ROWS];
+    uint32_t tot = 0;
+    if (r0 < n) {  // warp-uniform
+      // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
+      // lb (a second, offset load, mostly served by L1); one ballot per row.
+      K kr[FX_ROWS], kn[FX_ROWS];
 #pragma unroll
-    for (int j = 0; j < FX_ROWS; ++j) {
-      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-      const bool ok = i + 1 < n;
-      kr[j] = ok ? keys[i] : K(0);
-      kn[j] = ok ? keys[i + 1] : K(0);
-    }
-    // Does the run through r0 start before it?
-    bool carry = r0 > 0 && fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
-#pragma unroll
-    for (int j = 0; j < FX_ROWS; ++j) {
-      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-      const uint32_t dup = __ballot_sync(0xffffffffu, i + 1 < n && fx_same(kr[j], kn[j], lb));
-      const uint32_t starts = dup & ~((dup << 1) | (carry ? 1u : 0u));
-      carry = (dup >> 31) != 0;
-      if (starts) {  // warp-uniform
-        uint32_t at = 0;
-        if (lane == 0) at = atomicAdd(list_count, (uint32_t)__popc(starts));
-        at = __shfl_sync(0xffffffffu, at, 0);
-        if ((starts >> lane) & 1u) list[at + __popc(starts & ((1u << lane) - 1u))] = i;
+      for (int j = 0; j < FX_ROWS; ++j) {
+        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+        const bool ok = i + 1 < n;
+        kr[j] = ok ? keys[i] : K(0);
+        kn[j] = ok ? keys[i + 1] : K(0);
       }
+      // Does the run through r0 start before it?
+      bool carry = r0 > 0 && fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
+#pragma unroll
+      for (int j = 0; j < FX_ROWS; ++j) {
+        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+        const uint32_t dup = __ballot_sync(0xffffffffu, i + 1 < n && fx_same(kr[j], kn[j], lb));
+        st[j] = dup & ~((dup << 1) | (carry ? 1u : 0u));
+        carry = (dup >> 31) != 0;
+        tot += (uint32_t)__popc(st[j]);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < FX_ROWS; ++j) st[j] = 0;
     }
+    if (lane == 0) s_off[warp] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t sum = 0;
+#pragma unroll
+      for (int w = 0; w < WARPS; ++w) {
+        const uint32_t c = s_off[w];
+        s_off[w] = sum;
+        sum += c;
+      }
+      s_base = sum ? atomicAdd(list_count, sum) : 0u;
+    }
+    __syncthreads();
+    uint32_t at = s_base + s_off[warp];
+#pragma unroll
+    for (int j = 0; j < FX_ROWS; ++j) {
+      if ((st[j] >> lane) & 1u) list[at + (uint32_t)__popc(st[j] & lt)] = r0 + (uint32_t)j * 32 + lane;
+      at += (uint32_t)__popc(st[j]);
+    }
+    __syncthreads();  // s_off and s_base are read before the next round writes them
   }
 }
 
 // Sorts the listed runs: each lane the short run at one list entry, then the
 // warp the longer runs its lanes met, one by one.
 template <class K>
-__global__ void __launch_bounds__(FX_THREADS) run_sort_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
+__global__ void __launch_bounds__(FX_THREADS, 4) run_sort_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
                                                              uint32_t n, int lb, const uint32_t* __restrict__ list,
                                                              const uint32_t* list_count) {
   griddep_wait();
@@ -403,9 +445,17 @@ __global__ void __launch_bounds__(FX_THREADS) run_sort_kernel(K* keys, uint32_t*
     while (bal) {  // warp-uniform
       const uint32_t s = __shfl_sync(0xffffffffu, s0, __ffs(bal) - 1);
       bal &= bal - 1;
-      const K ks = keys[s];  // any key of the run: they share the high bits
-      uint32_t g = 0;        // run length: first key past s + 1 that differs above lb
-      for (uint32_t q0 = s + 2;; q0 += 32) {
+      // Keys s .. s + 31 in one load: the run's end if it holds at most 32
+      // keys, and then its keys as well.
+      const K kq = s + lane < n ? keys[s + lane] : K(0);
+      const K ks = (K)__shfl_sync(0xffffffffu, (unsigned long long)kq, 0);
+      const uint32_t b0 = __ballot_sync(0xffffffffu, s + lane >= n || !fx_same(kq, ks, lb));
+      if (b0) {
+        fx_short_run<K>(keys, vals, s, (uint32_t)(__ffs(b0) - 1), lb, kq);
+        continue;
+      }
+      uint32_t g = 0;  // run length: first key past s + 31 that differs above lb
+      for (uint32_t q0 = s + 32;; q0 += 32) {
         const uint32_t q = q0 + lane;
         const bool differs = q >= n || !fx_same(keys[q], ks, lb);
         const uint32_t bq = __ballot_sync(0xffffffffu, differs);
@@ -414,8 +464,7 @@ __global__ void __launch_bounds__(FX_THREADS) run_sort_kernel(K* keys, uint32_t*
           break;
         }
       }
-      if (g <= 32) fx_short_run<K>(keys, vals, s, g, lb);
-      else fx_long_run<K>(keys, vals, sk, sv, s, g, lb, s_cnt[warp]);
+      fx_long_run<K>(keys, vals, sk, sv, s, g, lb, s_cnt[warp]);
     }
   }
 }
@@ -424,9 +473,10 @@ template <class K>
 cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
                              uint32_t n, int low_bits, uint32_t* list, uint32_t* list_count) {
   if (n < 2) return cudaSuccess;
-  if (low_bits < 1 || low_bits > 16) return cudaErrorInvalidValue;  // two 8-bit passes at most
-  const uint32_t rows = ceil_div(n, (uint32_t)(FX_ROWS * 32));
-  const uint32_t grid = max(1u, min(ceil_div(rows, FX_THREADS / 32), (uint32_t)L.num_sms * 8));
+  if (low_bits < 1 || low_bits > 32 || low_bits >= (int)(8 * sizeof(K)))
+    return cudaErrorInvalidValue;  // run ranks hold 32 low bits, and some high bits must be sorted
+  const uint32_t chunks = ceil_div(n, (uint32_t)(FX_THREADS * FX_ROWS));
+  const uint32_t grid = max(1u, min(chunks, (uint32_t)L.num_sms * 8));
   cudaError_t e = launch_kernel(L, run_detect_kernel<K>, grid, FX_THREADS, 0, keys, n, low_bits, list, list_count);
   if (e != cudaSuccess) return e;
   return launch_kernel(L, run_sort_kernel<K>, (uint32_t)L.num_sms * 4, FX_THREADS, 0, keys, vals, scratch_keys,

@@ -240,8 +240,8 @@ typedef struct gtc_octree_buffers {
  * -> node offsets -> octree make+link, all stream-ordered with no host sync
  * (the commented pipeline of main.rs:60-170, with the GPU sort in place of the
  * CPU sort at main.rs:85).  key_bits = 32 or 64.  For 64-bit codes the sort
- * runs its passes over bits 16..62 and then sorts each run of codes equal in
- * those bits by bits 0..15: the same order as sorting all 63 bits. */
+ * runs its passes over bits 23..62 and then sorts each run of codes equal in
+ * those bits by bits 0..22: the same order as sorting all 63 bits. */
 GTC_API gtc_status gtc_build_octree(gtc_ctx* ctx, const float* pts, uint32_t n, float min_coord, float range,
                                     int key_bits, const gtc_octree_buffers* out, void* ws, size_t ws_bytes,
                                     gtc_stream_t stream);

@@ -55,12 +55,14 @@ def test_many_duplicates_3m(ctx, oracle, key_bits):
 
 
 def _cube_points(cubes, per_cube, seed):
-    """Points in cubes of side 2^-16 of the domain (5 low bits of each 21-bit
-    axis): the 64-bit codes of one cube agree in their top 48 bits.  With
-    per_cube = 0 each cube gets 5..60 points."""
+    """Points in cubes of side 2^-13 of the domain (8 low bits of each 21-bit
+    axis): the 64-bit codes of one cube agree in their top 39 bits, above
+    bit 24, and split into two runs of codes equal above bit 23, the bits the
+    sort leaves to its run fixup.  With per_cube = 0 each cube gets 5..60
+    points."""
     g = np.random.Generator(np.random.PCG64(seed))
-    side = 1024.0 / (1 << 16)
-    corners = np.floor(g.random((cubes, 3)) * (1 << 16)) * side
+    side = 1024.0 / (1 << 13)
+    corners = np.floor(g.random((cubes, 3)) * (1 << 13)) * side
     counts = np.full(cubes, per_cube) if per_cube else g.integers(5, 61, cubes)
     xyz = np.repeat(corners, counts, axis=0) + g.random((int(counts.sum()), 3)) * side
     out = np.ones((xyz.shape[0], 4), np.float32)
@@ -88,9 +90,10 @@ def test_edge_cases(ctx, oracle, key_bits):
         "line": p([[float(i) * 0.25, 1.0, 1.0] for i in range(4096)]),
         "ragged": W.uniform_points(123_457, seed=8),
         "dense_cluster": W.gaussian_mixture_points(200_000, 1, 0.05, seed=6),
-        # 64-bit codes that agree above bit 16 form runs the sort leaves to its
-        # run fixup: one run of 100K keys (the long path, across many tiles)
-        # and 2,000 runs of 5..60 keys (short and long paths at tile edges).
+        # 64-bit codes that agree above bit 23 form runs the sort leaves to its
+        # run fixup: two runs of about 50K keys (the long path, three counting
+        # passes, across many tiles) and 4,000 runs of about 2..30 keys (lane,
+        # warp and long paths at tile edges).
         "one_cell_run": _cube_points(1, 100_000, seed=31),
         "many_cell_runs": _cube_points(2_000, 0, seed=32),
     }
