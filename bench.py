@@ -350,7 +350,7 @@ def run_gtc(args):
     alg_total = sum(alg.values())
     ms_per_step = elapsed_ms / args.steps
     value = world * n / (ms_per_step * 1e-3) / 1e6
-    kernels_per_step = 1 + 5 + 2 + 1 + 2 + 1 + 1  # morton+hist, 5 passes, run detect + sort, unique, tree + long splits, scan, octree
+    kernels_per_step = 1 + 5 + 1 + 1 + 2 + 1 + 1  # morton+hist, 5 passes, run fixup, unique, tree + long splits, scan, octree
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
 
     line = {

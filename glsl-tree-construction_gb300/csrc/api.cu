@@ -183,7 +183,6 @@ size_t pipeline_ws_bytes(uint32_t n) {
   b += sort_workspace_bytes(n, passes, 0);
   b += 2 * scan_workspace_bytes(n);                   // unique, node offsets
   b += 256;                                           // long-range split and run counts
-  if (pipeline_begin_bit<K>()) b += align_up(((size_t)n / 2 + 1) * 4, 256);  // run starts
   return b;
 }
 
@@ -324,7 +323,7 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   w += scan_workspace_bytes(n);
   void* offsets_ws = w;
   w += scan_workspace_bytes(n);
-  uint32_t* q_count = reinterpret_cast<uint32_t*>(w);  // [0] long-range splits, [1] runs
+  uint32_t* q_count = reinterpret_cast<uint32_t*>(w);  // [0] long-range splits
   w += 256;
   K* keys = reinterpret_cast<K*>(o->keys);
   const SortWorkspace Wk = carve_sort_workspace(sort_ws, n, passes, 0);
@@ -333,7 +332,6 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
   // memset node sits between the kernels of the build.
   SortWorkspace Wz = Wk;
   Wz.desc_words = (size_t)(reinterpret_cast<uint32_t*>(w) - Wk.desc);
-  uint32_t* run_list = reinterpret_cast<uint32_t*>(w);  // not zeroed: written before read
   // Every kernel after the first starts under a programmatic dependent
   // launch (not while stage events are being recorded between them).
   Launch Lp = L;
@@ -371,7 +369,7 @@ gtc_status pipeline(gtc_ctx* ctx, const float* pts, uint32_t n, float mn, float 
     // The low bits decide only within runs of equal high bits: sort those
     // runs in place; the caller's pair of buffers is free as scratch.
     StageTimer t(ctx, stream, GTC_STAGE_RUN_FIXUP);
-    GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN, run_list, q_count + 1));
+    GTC_TRY(ctx, launch_run_fixup<K>(Lp, keys_alt, vals_alt, keys, o->idx, n, BEGIN));
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_UNIQUE);

@@ -450,10 +450,10 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
 // Completes a stable LSD sort over bits [low_bits, 64) into a sort of the
 // whole key: every run of keys that agree above low_bits is sorted stably by
 // its low bits (1 <= low_bits <= 32), in place; the scratch arrays hold n
-// entries, list holds n / 2 + 1 and *list_count is zero at the start.
+// entries.
 template <class K>
 cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
-                             uint32_t n, int low_bits, uint32_t* list, uint32_t* list_count);
+                             uint32_t n, int low_bits);
 
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,

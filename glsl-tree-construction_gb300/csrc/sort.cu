@@ -207,10 +207,10 @@ __global__ void __launch_bounds__(THREADS, 3) morton_hist_kernel(const float4* _
 // only among keys whose high digits tie.  For point-cloud Morton codes these
 // runs are short (277,486 runs of 2 to 20 keys in the 10M clustered codes
 // for lb = 23, 0.66M keys in all), so three 8-bit passes over every key
-// become one read of the keys and a few touches of 7% of them.  run_detect_kernel
-// streams the keys and lists every run start; run_sort_kernel takes the
-// list: a run of up to FX_LANE keys is sorted by one lane (all lanes at
-// once), up to 32 are ranked in registers by a warp, and longer runs are
+// become one read of the keys and a few touches of 7% of them.
+// run_fixup_kernel finds the runs of a chunk of keys per block and sorts
+// them: a run of up to FX_LANE keys is sorted by one lane (all lanes at
+// once), up to 31 are ranked in registers by a warp, and longer runs are
 // sorted by stable 8-bit counting passes through the scratch arrays (any
 // length, one warp, linear time).  Runs whose low bits are already in order
 // are left as they are.
@@ -358,88 +358,75 @@ __device__ void fx_long_run(K* keys, uint32_t* vals, K* sk, uint32_t* sv, uint32
   }
 }
 
-// Finds the runs: every position where a run of two or more keys starts is
-// appended to list (the order does not matter).  Each block takes 2,048
-// consecutive keys at a time and reserves its entries with one atomic: the
-// 10M clustered codes hold about one start per 20 keys, too many for a
-// counter taken per warp.
+// Finds and sorts the runs of one chunk of FX_THREADS * FX_ROWS = 2,048
+// consecutive keys per block.  Each warp streams eight rows of 32 keys (a
+// second, offset load for the next key, one ballot per row); a run starts
+// where key i + 1 agrees with key i above lb but key i - 1 does not.  The
+// block lists its starts in shared memory (at most one per two keys), then
+// its lanes take one listed run each: those keys were just read by this SM,
+// so the sort mostly hits L1.  A run belongs to the block holding its first
+// key and may reach into later chunks.  Blocks never write outside their own
+// runs, and what a block reads of a neighbour's run is the same whatever
+// order that run is in at the time (its keys agree above lb), so blocks run
+// in any order.
 template <class K>
-__global__ void __launch_bounds__(FX_THREADS) run_detect_kernel(const K* __restrict__ keys, uint32_t n, int lb,
-                                                               uint32_t* __restrict__ list, uint32_t* list_count) {
+__global__ void __launch_bounds__(FX_THREADS, 4) run_fixup_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
+                                                                 uint32_t n, int lb) {
   griddep_wait();
   constexpr int WARPS = FX_THREADS / 32;
-  constexpr uint32_t BLOCK_KEYS = WARPS * FX_ROWS * 32;
-  __shared__ uint32_t s_off[WARPS];
-  __shared__ uint32_t s_base;
+  constexpr uint32_t CHUNK = FX_THREADS * FX_ROWS;
+  __shared__ uint32_t s_list[CHUNK / 2];
+  __shared__ uint32_t s_tot[WARPS];
+  __shared__ uint32_t s_cnt[WARPS][256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
-  for (uint32_t b0 = blockIdx.x * BLOCK_KEYS; b0 < n; b0 += gridDim.x * BLOCK_KEYS) {  // block-uniform
-    const uint32_t r0 = b0 + (uint32_t)warp * FX_ROWS * 32;
-    uint32_t st[FX_ROWS];
-    uint32_t tot = 0;
-    if (r0 < n) {  // warp-uniform
-      // FX_ROWS rows in flight.  dup at i: key i + 1 agrees with key i above
-      // lb (a second, offset load, mostly served by L1); one ballot per row.
-      K kr[FX_ROWS], kn[FX_ROWS];
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j) {
-        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-        const bool ok = i + 1 < n;
-        kr[j] = ok ? keys[i] : K(0);
-        kn[j] = ok ? keys[i + 1] : K(0);
-      }
-      // Does the run through r0 start before it?
-      bool carry = r0 > 0 && fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j) {
-        const uint32_t i = r0 + (uint32_t)j * 32 + lane;
-        const uint32_t dup = __ballot_sync(0xffffffffu, i + 1 < n && fx_same(kr[j], kn[j], lb));
-        st[j] = dup & ~((dup << 1) | (carry ? 1u : 0u));
-        carry = (dup >> 31) != 0;
-        tot += (uint32_t)__popc(st[j]);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < FX_ROWS; ++j) st[j] = 0;
-    }
-    if (lane == 0) s_off[warp] = tot;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t sum = 0;
-#pragma unroll
-      for (int w = 0; w < WARPS; ++w) {
-        const uint32_t c = s_off[w];
-        s_off[w] = sum;
-        sum += c;
-      }
-      s_base = sum ? atomicAdd(list_count, sum) : 0u;
-    }
-    __syncthreads();
-    uint32_t at = s_base + s_off[warp];
+  const uint32_t r0 = blockIdx.x * CHUNK + (uint32_t)warp * FX_ROWS * 32;
+  uint32_t st[FX_ROWS];
+  uint32_t tot = 0;
+  if (r0 < n) {  // warp-uniform
+    K kr[FX_ROWS], kn[FX_ROWS];
 #pragma unroll
     for (int j = 0; j < FX_ROWS; ++j) {
-      if ((st[j] >> lane) & 1u) list[at + (uint32_t)__popc(st[j] & lt)] = r0 + (uint32_t)j * 32 + lane;
-      at += (uint32_t)__popc(st[j]);
+      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+      const bool ok = i + 1 < n;
+      kr[j] = ok ? keys[i] : K(0);
+      kn[j] = ok ? keys[i + 1] : K(0);
     }
-    __syncthreads();  // s_off and s_base are read before the next round writes them
+    // Does the run through r0 start before it?
+    bool carry = r0 > 0 && fx_same(keys[r0 - 1], keys[r0], lb);  // warp-uniform, two broadcast loads
+#pragma unroll
+    for (int j = 0; j < FX_ROWS; ++j) {
+      const uint32_t i = r0 + (uint32_t)j * 32 + lane;
+      const uint32_t dup = __ballot_sync(0xffffffffu, i + 1 < n && fx_same(kr[j], kn[j], lb));
+      st[j] = dup & ~((dup << 1) | (carry ? 1u : 0u));
+      carry = (dup >> 31) != 0;
+      tot += (uint32_t)__popc(st[j]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < FX_ROWS; ++j) st[j] = 0;
   }
-}
-
-// Sorts the listed runs: each lane the short run at one list entry, then the
-// warp the longer runs its lanes met, one by one.
-template <class K>
-__global__ void __launch_bounds__(FX_THREADS, 4) run_sort_kernel(K* keys, uint32_t* vals, K* sk, uint32_t* sv,
-                                                             uint32_t n, int lb, const uint32_t* __restrict__ list,
-                                                             const uint32_t* list_count) {
-  griddep_wait();
-  __shared__ uint32_t s_cnt[FX_THREADS / 32][256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t gw = blockIdx.x * (FX_THREADS / 32) + warp, nw = gridDim.x * (FX_THREADS / 32);
-  const uint32_t cnt = *list_count;
-  for (uint32_t base = gw * 32; base < cnt; base += nw * 32) {  // warp-uniform
-    const uint32_t e = base + lane;
-    const uint32_t s0 = e < cnt ? list[e] : 0u;
-    const bool longer = e < cnt && !fx_lane_run<K>(keys, vals, s0, n, lb);
+  if (lane == 0) s_tot[warp] = tot;
+  __syncthreads();
+  uint32_t at = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) {
+    const uint32_t c = s_tot[w];
+    at += w < warp ? c : 0u;
+    total += c;
+  }
+#pragma unroll
+  for (int j = 0; j < FX_ROWS; ++j) {
+    if ((st[j] >> lane) & 1u) s_list[at + (uint32_t)__popc(st[j] & lt)] = r0 + (uint32_t)j * 32 + lane;
+    at += (uint32_t)__popc(st[j]);
+  }
+  __syncthreads();
+  // Each lane the short run at one list entry, then the warp the longer
+  // runs its lanes met, one by one.
+  for (uint32_t e0 = (uint32_t)warp * 32; e0 < total; e0 += FX_THREADS) {  // warp-uniform
+    const uint32_t e = e0 + lane;
+    const uint32_t s0 = e < total ? s_list[e] : 0u;
+    const bool longer = e < total && !fx_lane_run<K>(keys, vals, s0, n, lb);
     __syncwarp();  // the lanes' writes are visible to the warp
     uint32_t bal = __ballot_sync(0xffffffffu, longer);
     while (bal) {  // warp-uniform
@@ -471,21 +458,18 @@ __global__ void __launch_bounds__(FX_THREADS, 4) run_sort_kernel(K* keys, uint32
 
 template <class K>
 cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratch_keys, uint32_t* scratch_vals,
-                             uint32_t n, int low_bits, uint32_t* list, uint32_t* list_count) {
+                             uint32_t n, int low_bits) {
   if (n < 2) return cudaSuccess;
   if (low_bits < 1 || low_bits > 32 || low_bits >= (int)(8 * sizeof(K)))
     return cudaErrorInvalidValue;  // run ranks hold 32 low bits, and some high bits must be sorted
-  const uint32_t chunks = ceil_div(n, (uint32_t)(FX_THREADS * FX_ROWS));
-  const uint32_t grid = max(1u, min(chunks, (uint32_t)L.num_sms * 8));
-  cudaError_t e = launch_kernel(L, run_detect_kernel<K>, grid, FX_THREADS, 0, keys, n, low_bits, list, list_count);
-  if (e != cudaSuccess) return e;
-  return launch_kernel(L, run_sort_kernel<K>, (uint32_t)L.num_sms * 4, FX_THREADS, 0, keys, vals, scratch_keys,
-                       scratch_vals, n, low_bits, list, list_count);
+  const uint32_t grid = ceil_div(n, (uint32_t)(FX_THREADS * FX_ROWS));
+  return launch_kernel(L, run_fixup_kernel<K>, grid, FX_THREADS, 0, keys, vals, scratch_keys, scratch_vals, n,
+                       low_bits);
 }
 template cudaError_t launch_run_fixup<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t,
-                                                int, uint32_t*, uint32_t*);
+                                                int);
 template cudaError_t launch_run_fixup<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*, uint32_t,
-                                                int, uint32_t*, uint32_t*);
+                                                int);
 
 // ------------------------------------------------------------ onesweep ----
 template <class K, int THREADS, int KPT>
