@@ -52,15 +52,17 @@ __device__ __forceinline__ void set_child(int4& lo, int4& hi, int w, int32_t v) 
   hi.w = (w == 7) ? v : hi.w;
 }
 
-// One 64-byte node as four 16-byte stores.
+// One 64-byte node as four 16-byte streaming stores: nothing in the build
+// reads the nodes back, so they are marked to leave L2 first and the radix
+// tree arrays the octree gathers from stay cached longer.
 __device__ __forceinline__ void store_node(gtc_octnode* nodes, uint32_t slot, int4 a, int4 b, float4 corner,
                                            float cell, int32_t nmask, int32_t lmask) {
   int4* p = reinterpret_cast<int4*>(nodes + slot);
-  p[0] = a;
-  p[1] = b;
-  p[2] = make_int4(__float_as_int(corner.x), __float_as_int(corner.y), __float_as_int(corner.z),
-                   __float_as_int(corner.w));
-  p[3] = make_int4(__float_as_int(cell), nmask, lmask, 0);
+  __stcs(p + 0, a);
+  __stcs(p + 1, b);
+  __stcs(p + 2, make_int4(__float_as_int(corner.x), __float_as_int(corner.y), __float_as_int(corner.z),
+                          __float_as_int(corner.w)));
+  __stcs(p + 3, make_int4(__float_as_int(cell), nmask, lmask, 0));
 }
 
 // D18: a single distinct key gives one root node without children.
