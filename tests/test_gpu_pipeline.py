@@ -70,6 +70,44 @@ def _cube_points(cubes, per_cube, seed):
     return out[g.permutation(out.shape[0])]
 
 
+def _box_runs(lengths, seed):
+    """One box of 2^8 x 2^8 x 2^7 finest cells per length (the x and y low
+    8 bits and the z low 7 bits free, at distinct box positions): the 64-bit
+    codes of a box agree in exactly bits 23..62, so each box is one run of
+    that many distinct keys for the run fixup, in shuffled input order."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    nb = len(lengths)
+    bx = g.choice(1 << 13, nb, replace=False)
+    by = g.integers(0, 1 << 13, nb)
+    bz = g.integers(0, 1 << 14, nb)
+    parts = []
+    for b, n_box in enumerate(lengths):
+        cells = g.choice(256 * 256 * 128, n_box, replace=False)
+        cx = bx[b] * 256 + (cells & 255)
+        cy = by[b] * 256 + ((cells >> 8) & 255)
+        cz = bz[b] * 128 + (cells >> 16)
+        parts.append((np.stack([cx, cy, cz], 1).astype(np.float64) + 0.5) * (1024.0 / (1 << 21)))
+    xyz = np.concatenate(parts)
+    out = np.ones((xyz.shape[0], 4), np.float32)
+    out[:, :3] = xyz  # exact: cell centres are multiples of 2^-12 below 1024
+    return out[g.permutation(out.shape[0])]
+
+
+def test_run_fixup_lengths(ctx, oracle):
+    """Runs of exactly the lengths where the run fixup changes path (one lane
+    up to 8 keys, a warp up to 31, counting passes from 32) and around the
+    2,048-key chunks its blocks own, three of each: 12 of them cross a chunk
+    boundary."""
+    lengths = (list(range(2, 13)) + [16, 30, 31, 32, 33, 34, 63, 64, 65, 100, 2047, 2048, 2049, 4100]) * 3
+    pts = _box_runs(lengths, seed=41)
+    codes = oracle.morton(pts, 64).view(np.uint64)
+    high = np.sort(codes) >> np.uint64(23)
+    edges = np.diff(np.concatenate(([0], (high[1:] == high[:-1]).astype(np.int8), [0])))
+    runs = np.flatnonzero(edges == -1) - np.flatnonzero(edges == 1) + 1
+    assert sorted(runs.tolist()) == sorted(lengths)  # the construction holds
+    _run(ctx, oracle, pts, 64, "fixup_lengths")
+
+
 @pytest.mark.parametrize("key_bits", [32, 64])
 def test_edge_cases(ctx, oracle, key_bits):
     def p(xyz):
