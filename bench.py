@@ -65,6 +65,48 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def init_replicas(world):
+    """Under torchrun every rank builds its own cloud on its own GPU (replicas,
+    no data exchange): a gloo group serves only the barriers around the timed
+    region and the max over ranks.  None for a single process."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(pg, value):
+    """The slowest rank's figure (the whole job ends with it); value itself
+    for a single process."""
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, value):
+    """The total over all ranks (units the whole job processes); value itself
+    for a single process."""
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def job_rate(units, ms_per_step):
+    """Whole-job throughput in millions of units per second: the units all
+    ranks process in one step over the slowest rank's step time."""
+    return units / (ms_per_step * 1e-3) / 1e6
+
+
 def measured_hbm_peak():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -209,12 +251,7 @@ def run_gtc(args):
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
     dev = f"cuda:{local}"
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
-        pg = dist
+    pg = init_replicas(world)
 
     n = args.n
     pts_np = W.config2_points(n, seed=rank)
@@ -277,10 +314,7 @@ def run_gtc(args):
     elapsed_ms = g0.elapsed_time(g1)
     clocks = clk.summary()
     ctx.device_status()
-    if pg:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(pg, elapsed_ms)
     graph_ms = elapsed_ms / args.steps
 
     # --- end to end through the host-buffer entry point (pinned host memory)
@@ -349,7 +383,7 @@ def run_gtc(args):
     alg = algorithmic_bytes(n, u, m, o, 8)
     alg_total = sum(alg.values())
     ms_per_step = elapsed_ms / args.steps
-    value = world * n / (ms_per_step * 1e-3) / 1e6
+    value = job_rate(world * n, ms_per_step)  # every rank builds an n-point cloud
     kernels_per_step = 1 + 5 + 1 + 1 + 2 + 1 + 1  # morton+hist, 5 passes, run fixup, unique, tree + long splits, scan, octree
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
 
@@ -601,12 +635,7 @@ def run_gtc_batched(args):
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
-        pg = dist
+    pg = init_replicas(world)
     S = args.clouds
     pts_np, offs_np = W.config4_clouds(S, seed=rank)
     n = pts_np.shape[0]
@@ -655,10 +684,8 @@ def run_gtc_batched(args):
     elapsed_ms = g0.elapsed_time(g1)
     clocks = clk.summary()
     ctx.device_status()
-    if pg:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(pg, elapsed_ms)
+    n_job = sum_over_ranks(pg, n)  # the ranks' clouds differ (seed = rank)
     graph_ms = elapsed_ms / args.steps
 
     # End to end: pinned host points in, every cloud's octree nodes out.
@@ -688,7 +715,7 @@ def run_gtc_batched(args):
     stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
     sizes = np.diff(offs_np.astype(np.int64))
     line = {
-        "metric": "Mpoints/s batched octree build", "value": round(world * n / (ms_per_step * 1e-3) / 1e6, 2),
+        "metric": "Mpoints/s batched octree build", "value": round(job_rate(n_job, ms_per_step), 2),
         "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
