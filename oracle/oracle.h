@@ -7,14 +7,23 @@
  * its `--impl reference` arm) may load it.  The product library never links,
  * loads or calls it, and nothing in the product falls back to it.
  *
- * Parity status: the reference (Rust host + GLSL compute shaders) cannot be
- * built or run here (no Rust toolchain, no graphics stack) and ships no tests
- * or golden vectors.  The one recorded output that can be checked, the global
- * digit histogram of `test_radix_sort` (radixsort-vulkan/output.txt:7684-8707),
- * is reproduced exactly by orc_global_hist_u32(..., ORC_LITERAL_D11) up to a
- * constant offset of 9n on every bin d >= 1 (see tests/test_oracle_pin.py).
- * Every other stage is "parity unpinned": it restates the shader math with the
- * reference-intent corrections listed below.
+ * Parity status: pinned to the reference's own code.  The reference (Rust
+ * host + GLSL compute shaders) cannot run here (no Rust toolchain, no
+ * graphics stack), but its shader function bodies are C-like:
+ * oracle/ref_shaders.py compiles the function bodies of morton.comp,
+ * unique.comp, build_radix_tree.comp, edge_count.comp, partial_sum.comp and
+ * octree.comp as written, as C++ on the CPU (oracle/_ref/, with ref_glue.cpp supplying the
+ * GLSL names and the host steps of main.rs:60-170), once per set of named
+ * deviation patches.  tests/test_oracle_ref_pin.py checks every stage here
+ * against that build byte for byte: the corrected forms against the fully
+ * patched shaders, each ORC_LITERAL_* switch against the shaders with that one
+ * deviation left in, and the 64-bit forms against the shaders with 64-bit
+ * codes substituted.  tests/golden/ref_pipeline_{32,64}.npz hold that build's
+ * outputs for machines without the reference checkout.  The global digit
+ * histogram of `test_radix_sort` (output.txt:7684-8707) is reproduced by
+ * orc_global_hist_u32(..., ORC_LITERAL_D11) up to a constant offset of 9n on
+ * every bin d >= 1 (tests/test_oracle_pin.py).  The 64-bit Morton encode has
+ * no reference counterpart and is checked against known answers.
  *
  * Reference-intent corrections (default) and the switches that restore the
  * literal form where the literal form is deterministic:

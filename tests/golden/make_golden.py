@@ -5,11 +5,18 @@
    histogram.rs:265-267 after histogram.comp ran over the keys 10,000,000..1 of
    test_radix_sort, main.rs:189-190).  Needs the reference checkout (read as
    text only); the fixture is committed so tests never read the reference.
-2. oracle_small_{32,64}.npz - inputs and every stage output of the oracle on
+2. ref_pipeline_{32,64}.npz - inputs and every stage output of the
+   reference's own shaders (oracle/_ref/libref_shaders.so, built from the
+   checkout by oracle/ref_shaders.py) driven in main.rs:60-170's order with
+   the deviation patches applied: reference-derived vectors that the oracle
+   and the CUDA path are checked against on machines without the checkout.
+   64-bit codes are not in the reference: that fixture runs the shaders with
+   64-bit codes substituted, on codes from the oracle's 64-bit encode.
+3. oracle_small_{32,64}.npz - inputs and every stage output of the oracle on
    small seeded inputs, so the oracle built on another machine (the GPU host
    is aarch64) can be checked against the one that produced these.
 
-Usage: python tests/golden/make_golden.py [path-to-reference-checkout]
+Usage: python tests/golden/make_golden.py <path-to-reference-checkout>
 """
 from __future__ import annotations
 
@@ -40,6 +47,31 @@ def make_ref_hist(ref_root: str) -> None:
             f.write(f"{vals[i]}\n")
 
 
+REF_CASES = {
+    32: ("uniform 2^14 points, seed 3", lambda W: W.uniform_points(1 << 14, seed=3)),
+    64: ("8-component mixture, sigma 2, 2% noise, 2^14 points, seed 5",
+         lambda W: W.gaussian_mixture_points(1 << 14, 8, 2.0, noise=0.02, seed=5)),
+}
+
+
+def make_ref_vectors(ref_root: str) -> None:
+    import oracle as O
+    from oracle import ref as R
+    from gtc import workloads as W
+
+    O.build()
+    R.build(ref_root)
+    for kb, (what, gen) in REF_CASES.items():
+        pts = gen(W)
+        out = R.build_octree(pts if kb == 32 else O.morton(pts, 64), kb)
+        np.savez_compressed(
+            os.path.join(HERE, f"ref_pipeline_{kb}.npz"), what=np.array(what), pts=pts, keys=out["keys"],
+            idx=out["idx"], prefix_n=out["prefix_n"], has_leaf_left=out["has_leaf_left"],
+            has_leaf_right=out["has_leaf_right"], left_child=out["left_child"], parent=out["parent"],
+            edge_count=out["edge_count"], node_offsets=out["node_offsets"],
+            nodes=out["nodes"].view(np.int32).reshape(-1, 16))
+
+
 def make_oracle_vectors() -> None:
     import oracle as O
     from gtc import workloads as W
@@ -55,8 +87,9 @@ def make_oracle_vectors() -> None:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if os.path.isdir(ref):
-        make_ref_hist(ref)
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    make_ref_hist(sys.argv[1])
+    make_ref_vectors(sys.argv[1])
     make_oracle_vectors()
     print("fixtures written to", HERE)

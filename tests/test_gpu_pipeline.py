@@ -272,3 +272,26 @@ def test_deterministic_across_runs(ctx):
     a = gtc.build_octree(ctx, pts, 64)
     b = gtc.build_octree(ctx, pts, 64)
     assert torch.equal(a.nodes, b.nodes) and torch.equal(a.keys, b.keys) and torch.equal(a.idx, b.idx)
+
+
+@pytest.mark.parametrize("key_bits", [32, 64])
+def test_reference_fixture(ctx, key_bits):
+    """The CUDA build against the reference's own shaders' outputs
+    (tests/golden/ref_pipeline_{32,64}.npz, recorded from the shader code
+    compiled on the CPU, in main.rs:60-170's order), byte for byte."""
+    import os
+
+    import gtc
+    import torch
+
+    fx = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", f"ref_pipeline_{key_bits}.npz")))
+    res = gtc.build_octree(ctx, torch.from_numpy(fx["pts"]).cuda(), key_bits)
+    kd = np.uint32 if key_bits == 32 else np.uint64
+    assert (res.n_unique, res.n_oct_nodes) == (fx["keys"].size, fx["nodes"].shape[0])
+    for name, t, dt in [("keys", res.keys, kd), ("idx", res.idx, np.uint32), ("prefix_n", res.prefix_n, np.uint8),
+                        ("has_leaf_left", res.has_leaf_left, np.uint8),
+                        ("has_leaf_right", res.has_leaf_right, np.uint8), ("left_child", res.left_child, np.int32),
+                        ("parent", res.parent, np.int32), ("edge_count", res.edge_count, np.uint32),
+                        ("node_offsets", res.node_offsets, np.uint32)]:
+        assert np.array_equal(t.cpu().numpy().view(dt), fx[name]), name
+    assert np.array_equal(gtc.nodes_to_numpy(res.nodes).view(np.int32).reshape(-1, 16), fx["nodes"])
