@@ -107,6 +107,13 @@ def job_rate(units, ms_per_step):
     return units / (ms_per_step * 1e-3) / 1e6
 
 
+def replica_rate(pg, units, seconds):
+    """Whole-job rate of a figure every rank measures on its own (an end-to-end
+    loop): all ranks' units over the slowest rank's seconds, in millions of
+    units per second."""
+    return job_rate(sum_over_ranks(pg, units), max_over_ranks(pg, seconds) * 1e3)
+
+
 def measured_hbm_peak():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -354,7 +361,8 @@ def run_gtc(args):
     for i in range(q_steps):
         ctx.check(L.gtc_build_octree_host_async(ctx.h, hp, n, 0.0, 1024.0, KEY_BITS, outs[i % NQ], cap, hc[i % NQ]))
     ctx.check(L.gtc_build_octree_host_wait(ctx.h))
-    e2e_s = (time.perf_counter() - t0) / q_steps
+    e2e_rate = replica_rate(pg, n, (time.perf_counter() - t0) / q_steps)
+    e2e_sync_rate = replica_rate(pg, n, e2e_sync_s)
     for c in hc:
         got = np.ctypeslib.as_array((ctypes.c_uint32 * 3).from_address(c.value))
         assert tuple(int(x) for x in got) == (u, m, o)
@@ -406,11 +414,11 @@ def run_gtc(args):
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "bytes_per_launch": pass_bytes, "avg_launch_ms": round(avg_pass_ms, 5)},
-        "e2e": {"value": round(n / e2e_s / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": n * 16,
+        "e2e": {"value": round(e2e_rate, 2), "unit": UNIT, "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": o * 64 + 12,
                 "api": "gtc_build_octree_host_async x steps + gtc_build_octree_host_wait (pinned host buffers, "
                        "consecutive builds overlapped)",
-                "sync_value": round(n / e2e_sync_s / 1e6, 2),
+                "sync_value": round(e2e_sync_rate, 2),
                 "sync_api": "gtc_build_octree_host, one build at a time"},
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
@@ -701,7 +709,7 @@ def run_gtc_batched(args):
         plan.launch(dp, offs)
         hn.copy_(plan.nodes[:o], non_blocking=True)
         torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_rate = replica_rate(pg, n, (time.perf_counter() - t0) / e2e_steps)
     ctx.device_status()
     if rank != 0:
         return
@@ -730,7 +738,7 @@ def run_gtc_batched(args):
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": None, "peak_kind": peak_kind, "bytes_per_launch": pass_bytes,
                      "avg_launch_ms": round(avg_pass_ms, 5)},
-        "e2e": {"value": round(n / e2e_s / 1e6, 2), "unit": "Mpoints/s", "h2d_bytes_per_step": n * 16,
+        "e2e": {"value": round(e2e_rate, 2), "unit": "Mpoints/s", "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": o * 64, "api": "gtc_build_octree_batched between pinned host copies"},
         "gpu_launches": 13 * args.steps,
         "clocks": clocks,

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -19,6 +20,45 @@ void sort_variant_shape(int v, int* threads, int* kpt);
 
 static std::atomic<uint32_t> g_literal{0};
 uint32_t literal_flags() { return g_literal.load(std::memory_order_relaxed); }
+
+namespace setup_cache {
+struct SetupKey {
+  int device;
+  const void* kern;
+  int threads;
+  size_t smem;
+  bool operator<(const SetupKey& o) const {
+    if (device != o.device) return device < o.device;
+    if (kern != o.kern) return kern < o.kern;
+    if (threads != o.threads) return threads < o.threads;
+    return smem < o.smem;
+  }
+};
+std::mutex g_setup_mu;
+std::map<SetupKey, int> g_setup;  // resident blocks per SM, per device and kernel shape
+}  // namespace setup_cache
+using namespace setup_cache;
+
+cudaError_t kernel_setup(const void* kern, int threads, size_t smem, int* blocks_per_sm) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const SetupKey key{dev, kern, threads, smem};
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  auto it = g_setup.find(key);
+  if (it == g_setup.end()) {
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    it = g_setup.emplace(key, occ > 0 ? occ : 1).first;
+  }
+  if (blocks_per_sm) *blocks_per_sm = it->second;
+  return cudaSuccess;
+}
 }  // namespace gtc
 
 using namespace gtc;
@@ -108,6 +148,9 @@ gtc_status fail(gtc_ctx* ctx, gtc_status s, const char* what, cudaError_t e = cu
 inline cudaStream_t S(gtc_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline Launch launch_of(gtc_ctx* ctx, gtc_stream_t s) { return Launch{S(s), ctx->d_status, ctx->num_sms}; }
+
+// Clears status bits atomically, keeping every flag other builds raised.
+__global__ void clear_status_bits_kernel(uint32_t* status, uint32_t bits) { atomicAnd(status, ~bits); }
 
 cudaEvent_t get_event(gtc_ctx* ctx) {
   if (!ctx->free_events.empty()) {
@@ -436,6 +479,7 @@ gtc_status ensure_resident(gtc_ctx* ctx, Resident& r, uint32_t n, int key_bits, 
 namespace gtc {
 // Accessors for entry points defined in other translation units.
 Launch context_launch(gtc_ctx* ctx, gtc_stream_t stream) { return launch_of(ctx, stream); }
+int context_device(const gtc_ctx* ctx) { return ctx->device; }
 gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_t e) { return fail(ctx, s, msg, e); }
 cudaEvent_t context_stage_begin(gtc_ctx* ctx, gtc_stream_t stream) {
   if (!ctx->profiling) return nullptr;
@@ -762,7 +806,10 @@ GTC_API gtc_status gtc_build_octree_host(gtc_ctx* ctx, const float* host_pts, ui
     GTC_TRY(ctx, cudaStreamSynchronize(st));
     const uint32_t o = c[2];
     if (o > r.nodes_cap) {  // rare: long single-child chains; grow and rebuild
-      cudaMemsetAsync(ctx->d_status, 0, 4, st);
+      // Clear only the capacity flag this build raised: the status word is
+      // shared with queued builds, whose other flags (a timeout) must stay.
+      clear_status_bits_kernel<<<1, 1, 0, st>>>(ctx->d_status, DEV_CAPACITY);
+      GTC_TRY(ctx, cudaGetLastError());
       s = ensure_resident(ctx, ctx->res, n, key_bits, o);
       if (s != GTC_OK) return s;
       continue;
@@ -787,7 +834,10 @@ static gtc_status queue_readback(gtc_ctx* ctx, int q) {
   out.pending = false;
   GTC_TRY(ctx, cudaEventSynchronize(ctx->qbuilt[q]));
   const uint32_t o = out.counts[2];
-  if (o > ctx->qres[q].nodes_cap) return GTC_OK;  // the build flagged DEV_CAPACITY; the wait reports it
+  if (o > ctx->qres[q].nodes_cap) {  // the device node buffer was too small: reported by the wait
+    if (ctx->qerr == GTC_OK) ctx->qerr = fail(ctx, GTC_ERR_CAPACITY, "octree node capacity of a queued build");
+    return GTC_OK;
+  }
   if (!out.nodes) return GTC_OK;                   // counts only
   if (o > out.cap) {
     if (ctx->qerr == GTC_OK) ctx->qerr = fail(ctx, GTC_ERR_CAPACITY, "host node buffer too small");

@@ -684,11 +684,7 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   do {                                                                            \
     if ((e = (x)) != cudaSuccess) return context_error(ctx, GTC_ERR_CUDA, #x, e); \
   } while (0)
-  static bool attr = false;  // set once, outside any graph capture
-  if (!attr) {
-    BCHK(cudaFuncSetAttribute(bt_onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BtSmem)));
-    attr = true;
-  }
+  BCHK(kernel_setup(bt_onesweep_kernel, BT_THREADS, sizeof(BtSmem)));
   if (n_total == 0) {
     BCHK(cudaMemsetAsync(out->key_offset, 0, ((size_t)S + 1) * 4, s));
     BCHK(cudaMemsetAsync(out->node_offset, 0, ((size_t)S + 1) * 4, s));
@@ -731,10 +727,8 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
     uint32_t* uws = reinterpret_cast<uint32_t*>(W.scan_ws);
     // The resident segment form once the batch fills the GPU; its
     // descriptors fit the workspace's tile count.
-    static int occ = 0;  // resident blocks per SM, queried once
-    if (occ == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bt_chunk_unique_kernel, CS_THREADS, 0) !=
-                         cudaSuccess ||
-                     occ < 1)) {
+    int occ = 1;  // resident blocks per SM
+    if (kernel_setup(bt_chunk_unique_kernel, CS_THREADS, 0, &occ) != cudaSuccess) {
       cudaGetLastError();
       occ = 1;
     }
@@ -783,10 +777,8 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   }
   {
     Stage t(ctx, stream, GTC_STAGE_OCTREE);
-    static int occ = 0;  // resident blocks per SM, queried once
-    if (occ == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bt_octree_kernel, BT_OCT_THREADS, 0) !=
-                         cudaSuccess ||
-                     occ < 1)) {
+    int occ = 4;  // resident blocks per SM
+    if (kernel_setup(bt_octree_kernel, BT_OCT_THREADS, 0, &occ) != cudaSuccess) {
       cudaGetLastError();
       occ = 4;
     }

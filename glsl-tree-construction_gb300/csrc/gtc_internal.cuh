@@ -393,6 +393,20 @@ __device__ __forceinline__ void griddep_wait() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Per-device kernel set-up.  The dynamic shared memory opt-in
+// (cudaFuncSetAttribute) and the resident-blocks answer belong to the device
+// that is current when they are made, so they are cached per device: one entry
+// per (current device, kernel, block size, dynamic shared bytes), read and
+// filled under a mutex because several host threads may launch at once.  The
+// first launch of a kernel shape on a device does the set-up; later ones only
+// read the cache.  smem above the 48 KB default gets the opt-in;
+// blocks_per_sm (nullable) receives the occupancy answer (at least 1).
+cudaError_t kernel_setup(const void* kern, int threads, size_t smem, int* blocks_per_sm);
+template <class... P>
+cudaError_t kernel_setup(void (*kern)(P...), int threads, size_t smem, int* blocks_per_sm = nullptr) {
+  return kernel_setup(reinterpret_cast<const void*>(kern), threads, smem, blocks_per_sm);
+}
+
 // Kernel launch honouring Launch::pdl (cudaLaunchKernelEx with the
 // programmatic stream serialization attribute).
 template <class... P, class... A>

@@ -846,8 +846,7 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
   const int B = m->B;
   LTRY(ctx, cudaMemsetAsync(d_counts, 0, (size_t)B * 4, s));
   if (n == 0) return GTC_OK;
-  LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)model_smem_bytes(MAX_BUCKETS)));
+  LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, model_smem_bytes(MAX_BUCKETS)));
   learned_count_kernel<<<ceil_div(n, LC_TILE), LC_THREADS, model_smem_bytes(B), s>>>(keys, n, m->knots, m->heights, B,
                                                                                      d_counts, nullptr);
   LTRY(ctx, cudaGetLastError());
@@ -878,18 +877,10 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
   const size_t msmem = model_smem_bytes(B);
   const int lb = 31 - __builtin_clz((unsigned)B);  // bucket-id bits
   const int db1 = (lb + 1) / 2, db2 = lb - db1;      // digit widths of the two passes (<= 7 each)
-  static bool attr = false;
-  if (!attr) {
-    LTRY(ctx, cudaFuncSetAttribute(learned_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)model_smem_bytes(MAX_BUCKETS)));
-    LTRY(ctx, cudaFuncSetAttribute(learned_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(LpSmem)));
-    LTRY(ctx, cudaFuncSetAttribute(learned_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(LpSmem)));
-    LTRY(ctx, cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(BucketSmem)));
-    attr = true;
-  }
+  LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, model_smem_bytes(MAX_BUCKETS)));
+  LTRY(ctx, kernel_setup(learned_pass_kernel<true>, LP_THREADS, sizeof(LpSmem)));
+  LTRY(ctx, kernel_setup(learned_pass_kernel<false>, LP_THREADS, sizeof(LpSmem)));
+  LTRY(ctx, kernel_setup(bucket_sort_kernel, BS_THREADS, sizeof(BucketSmem)));
   const Launch L0 = context_launch(ctx, stream);
   LTRY(ctx, cudaMemsetAsync(W.misc, 0, 256, s));
   LTRY(ctx, cudaMemsetAsync(W.totals, 0, (size_t)B * 4, s));

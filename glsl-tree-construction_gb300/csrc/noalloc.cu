@@ -38,15 +38,12 @@ static __device__ __align__(256) unsigned char g_sort_scratch[NOALLOC_SCRATCH_BY
 static std::mutex g_scratch_mu;
 static void* g_scratch_addr[64] = {};
 
-static cudaError_t scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
+static cudaError_t scratch_address(int dev, void** out) {
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_scratch_mu);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = p;
   }
@@ -55,6 +52,7 @@ static cudaError_t scratch_address(void** out) {
 }
 
 Launch context_launch(gtc_ctx* ctx, gtc_stream_t stream);
+int context_device(const gtc_ctx* ctx);
 gtc_status context_error(gtc_ctx* ctx, gtc_status s, const char* msg, cudaError_t e);
 
 }  // namespace gtc
@@ -78,8 +76,16 @@ extern "C" GTC_API gtc_status gtc_sort_pairs_u32_noalloc(gtc_ctx* ctx, uint32_t*
   const int passes = (end_bit - begin_bit + 7) / 8;
   if (sort_workspace_bytes(n, passes, 0) > NOALLOC_SCRATCH_BYTES)
     return context_error(ctx, GTC_ERR_INVALID_ARG, "static scratch smaller than the sort layout", cudaSuccess);
+  // The scratch address belongs to the current device, the stream and the
+  // status word to the context's: the two must agree.
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return context_error(ctx, GTC_ERR_CUDA, "cudaGetDevice", e);
+  if (dev != context_device(ctx))
+    return context_error(ctx, GTC_ERR_INVALID_ARG,
+                         "gtc_sort_pairs_u32_noalloc: the context's device must be the current device", cudaSuccess);
   void* scratch = nullptr;
-  cudaError_t e = scratch_address(&scratch);
+  e = scratch_address(dev, &scratch);
   if (e != cudaSuccess) return context_error(ctx, GTC_ERR_CUDA, "cudaGetSymbolAddress(g_sort_scratch)", e);
 
   const Launch L = context_launch(ctx, stream);

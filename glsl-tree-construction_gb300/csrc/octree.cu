@@ -72,14 +72,11 @@ cudaError_t launch_octree_make(const Launch& L, const K* codes, const uint32_t* 
   if (work == 0) return cudaSuccess;
   // One resident wave; each warp walks many 32-node slices, so the partial
   // batch at its end is small.
-  static int resident[2] = {0, 0};  // blocks per SM of each instantiation, queried once
-  int& occ = resident[with_leaves ? 1 : 0];
-  if (occ == 0) {
-    const void* kern = with_leaves ? (const void*)octree_make_kernel<K, true> : (const void*)octree_make_kernel<K, false>;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, OCT_THREADS, 0) != cudaSuccess || occ < 1) {
-      cudaGetLastError();
-      occ = 4;
-    }
+  int occ = 4;  // blocks per SM
+  const void* kern = with_leaves ? (const void*)octree_make_kernel<K, true> : (const void*)octree_make_kernel<K, false>;
+  if (kernel_setup(kern, OCT_THREADS, 0, &occ) != cudaSuccess) {
+    cudaGetLastError();
+    occ = 4;
   }
   const uint32_t grid = max(1u, min(ceil_div(work, OCT_THREADS), (uint32_t)(L.num_sms * occ)));
   if (with_leaves)

@@ -229,18 +229,15 @@ __global__ void __launch_bounds__(CS_THREADS) chunk_unique_kernel(const K* __res
 
 // Blocks of a resident grid for the segment scans (0: use the single-pass
 // kernels).  Capped by the descriptor words of the workspace.
-// `resident` caches the kernel's resident block count (~0u: not yet known).
-static uint32_t chunk_grid(const Launch& L, const void* kern, uint32_t n_max, uint32_t* resident) {
-  if (*resident == ~0u) {
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, CS_THREADS, 0) != cudaSuccess || occ <= 0) {
-      cudaGetLastError();
-      occ = 0;
-    }
-    *resident = (uint32_t)occ * (uint32_t)L.num_sms;
+static uint32_t chunk_grid(const Launch& L, const void* kern, uint32_t n_max) {
+  int occ = 0;
+  if (kernel_setup(kern, CS_THREADS, 0, &occ) != cudaSuccess) {
+    cudaGetLastError();
+    return 0u;
   }
+  const uint32_t resident = (uint32_t)occ * (uint32_t)L.num_sms;
   const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);  // descriptor words cleared by the launcher
-  const uint32_t g = min(*resident, tiles);
+  const uint32_t g = min(resident, tiles);
   // Worth it once every warp has a few rows to stream.
   return (g >= 64 && (uint64_t)n_max >= (uint64_t)g * CS_WARPS * 256) ? g : 0u;
 }
@@ -347,10 +344,8 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
   if (e != cudaSuccess) return e;
   if (n == 0) return d_count ? cudaMemsetAsync(d_count, 0, 4, L.stream) : cudaSuccess;
   if (kin != kout && vin != vout) {
-    static uint32_t grid[2] = {~0u, ~0u};  // per instantiation, for n_max = n (queried once, before any capture)
-    const int hv = vin ? 1 : 0;
     const void* kern = vin ? (const void*)chunk_unique_kernel<K, true> : (const void*)chunk_unique_kernel<K, false>;
-    const uint32_t g = chunk_grid(L, kern, n, &grid[hv]);
+    const uint32_t g = chunk_grid(L, kern, n);
     if (g) {
       if (vin)
         return launch_kernel(L, chunk_unique_kernel<K, true>, g, CS_THREADS, 0, kin, vin, kout, vout, n, w, d_count,
@@ -360,22 +355,15 @@ cudaError_t launch_unique(const Launch& L, const K* kin, const uint32_t* vin, K*
     }
   }
   const size_t smem = sizeof(UniqueSmem<K>);
-  static bool attr_set[2] = {false, false};  // per instantiation: set once, outside any graph capture
   if (vin) {
     auto kern = unique_kernel<K, true>;
-    if (!attr_set[1]) {
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      attr_set[1] = true;
-    }
+    e = kernel_setup(kern, SCAN_THREADS, smem);
+    if (e != cudaSuccess) return e;
     return launch_kernel(L, kern, tiles, SCAN_THREADS, smem, kin, vin, kout, vout, n, w, d_count, L.status);
   } else {
     auto kern = unique_kernel<K, false>;
-    if (!attr_set[0]) {
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      attr_set[0] = true;
-    }
+    e = kernel_setup(kern, SCAN_THREADS, smem);
+    if (e != cudaSuccess) return e;
     return launch_kernel(L, kern, tiles, SCAN_THREADS, smem, kin, nullptr, kout, nullptr, n, w, d_count, L.status);
   }
 }
@@ -464,9 +452,8 @@ static cudaError_t launch_scan(const Launch& L, const uint32_t* in, uint32_t* ou
   const uint32_t tiles = ceil_div(n_max > 0 ? n_max : 1, SCAN_TILE);
   cudaError_t e = L.ws_zeroed ? cudaSuccess : cudaMemsetAsync(w, 0, (64 + (size_t)tiles) * 4, L.stream);
   if (e != cudaSuccess) return e;
-  static uint32_t grid = ~0u;
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
-  const uint32_t g = aligned ? chunk_grid(L, (const void*)chunk_scan_kernel, n_max, &grid) : 0u;
+  const uint32_t g = aligned ? chunk_grid(L, (const void*)chunk_scan_kernel, n_max) : 0u;
   if (g)
     return launch_kernel(L, chunk_scan_kernel, g, CS_THREADS, 0, in, out, count_host, d_u, node_offsets, w, d_o,
                          L.status);

@@ -19,6 +19,8 @@
 
 #include <cstdio>
 
+#include <atomic>
+
 #include "gtc_internal.cuh"
 
 namespace gtc {
@@ -888,12 +890,13 @@ constexpr Variant kVariants[] = {{256, 16, 0, 3, 1}, {384, 16, 0, 2, 1}, {512, 1
                                  {512, 8, 0, 2, 1},  {384, 12, 0, 3, 1}, {256, 16, 0, 3, 0}, {384, 16, 0, 2, 0},
                                  {512, 12, 0, 2, 0}, {256, 24, 0, 2, 0}, {256, 16, 4, 3, 1}, {512, 12, 4, 2, 0}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
-static int g_pinned[2] = {-1, -1};  // gtc_sort_set_variant: overrides the tuned choice
+static const int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
+static std::atomic<int> g_pinned[2] = {{-1}, {-1}};  // gtc_sort_set_variant: overrides the tuned choice
 
 int sort_select_variant(int key_bits, int bits, uint32_t n) {
   const int w = key_bits == 64;
-  if (g_pinned[w] >= 0) return g_pinned[w];
+  const int pinned = g_pinned[w].load(std::memory_order_relaxed);
+  if (pinned >= 0) return pinned;
   const int t = tuned_variant(key_bits, bits, n);
   return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
 }
@@ -904,12 +907,8 @@ static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin
                               uint32_t* tile_counter) {
   using S = OnesweepSmem<K, THREADS, KPT>;
   auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, EARLY, L2H>;
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  cudaError_t e = kernel_setup(kern, THREADS, sizeof(S));
+  if (e != cudaSuccess) return e;
   const uint32_t tiles = ceil_div(n, S::TILE);
   return launch_kernel(L, kern, tiles, THREADS, sizeof(S), kin, vin, kout, vout, n, shift, dmask, bin_off, desc,
                        tile_counter, L.status, L.run_if);
@@ -921,15 +920,9 @@ static cudaError_t launch_tma(const Launch& L, const K* kin, const uint32_t* vin
                               uint32_t* tile_counter) {
   using S = TmaSmem<K, THREADS, KPT, HV>;
   auto kern = onesweep_tma_kernel<K, THREADS, KPT, HV, MATCH>;
-  static int per_sm = 0;  // resident CTAs per SM, per instantiation
-  if (per_sm == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
-    if (e != cudaSuccess) return e;
-    int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, sizeof(S));
-    if (e != cudaSuccess) return e;
-    per_sm = occ > 0 ? occ : 1;
-  }
+  int per_sm = 1;  // resident CTAs per SM
+  cudaError_t e = kernel_setup(kern, THREADS, sizeof(S), &per_sm);
+  if (e != cudaSuccess) return e;
   const uint32_t tiles = ceil_div(n, S::TILE);
   const uint32_t grid = min(tiles, (uint32_t)(per_sm * L.num_sms));
   return launch_kernel(L, kern, grid, THREADS, sizeof(S), kin, vin, kout, vout, n, shift, dmask, bin_off, desc,
@@ -1034,13 +1027,10 @@ cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint
             : form == 2 ? morton_hist_kernel<K, T, 1, RUN_FIXUP_BITS>
                         : morton_hist_kernel<K, T, 2, RUN_FIXUP_BITS>;
   // One resident wave: every block loops over the points.
-  static int resident[4] = {0, 0, 0, 0};  // blocks per SM of each form, queried once
-  int& occ = resident[form];
-  if (occ == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, T, 0) != cudaSuccess || occ < 1) {
-      cudaGetLastError();
-      occ = 2;
-    }
+  int occ = 2;  // blocks per SM
+  if (kernel_setup(kern, T, 0, &occ) != cudaSuccess) {
+    cudaGetLastError();
+    occ = 2;
   }
   const uint32_t want = ceil_div(n, T * 8);
   const uint32_t grid = max(1u, min(want, (uint32_t)(L.num_sms * occ)));
@@ -1092,12 +1082,13 @@ template cudaError_t launch_onesweep_passes<uint64_t>(const Launch&, uint64_t*, 
 int sort_num_variants() { return kNumVariants; }
 int sort_get_variant(int key_bits) {
   const int w = key_bits == 64;
-  return g_pinned[w] >= 0 ? g_pinned[w] : g_variant[w];
+  const int pinned = g_pinned[w].load(std::memory_order_relaxed);
+  return pinned >= 0 ? pinned : g_variant[w];
 }
 // v = -1 unpins (back to tuned / default selection).
 bool sort_set_variant(int key_bits, int v) {
   if (v < -1 || v >= kNumVariants) return false;
-  g_pinned[key_bits == 64] = v;
+  g_pinned[key_bits == 64].store(v, std::memory_order_relaxed);
   return true;
 }
 void sort_variant_shape(int v, int* threads, int* kpt) {

@@ -9,6 +9,8 @@
 // the code loads go through the read-only L1 path, which serves the short
 // searches that make up most nodes.
 
+#include <atomic>
+
 #include "karras.cuh"
 #include "tree_window.cuh"
 
@@ -17,11 +19,11 @@ namespace gtc {
 constexpr int TREE_THREADS = 256;
 
 // 1: split-indexed window kernel (tree_window.cuh); 0: per-node Karras search.
-static int g_tree_method = 1;
-int tree_get_method() { return g_tree_method; }
+static std::atomic<int> g_tree_method{1};
+int tree_get_method() { return g_tree_method.load(std::memory_order_relaxed); }
 bool tree_set_method(int m) {
   if (m != 0 && m != 1) return false;
-  g_tree_method = m;
+  g_tree_method.store(m, std::memory_order_relaxed);
   return true;
 }
 
@@ -52,7 +54,7 @@ cudaError_t launch_radix_tree(const Launch& L, const K* codes, const uint32_t* d
                               uint32_t* edge, uint32_t* d_m, uint32_t* queue, uint32_t* q_count) {
   const uint32_t work = d_u ? n_max : (uint32_t)max(m_host, 0);
   if (work == 0 && !d_m) return cudaSuccess;
-  if (g_tree_method == 1) {
+  if (g_tree_method.load(std::memory_order_relaxed) == 1) {
     const uint32_t u_host = d_u ? 0u : (uint32_t)max(m_host, 0) + 1;
     if (queue && !L.ws_zeroed) {
       cudaError_t e = cudaMemsetAsync(q_count, 0, 4, L.stream);

@@ -330,10 +330,11 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
  * Its scratch is a fixed 4,210,944-byte array inside the library, held by
  * every GPU that loads the library until the process exits, so n is limited
  * to GTC_NOALLOC_MAX_KEYS (larger n returns GTC_ERR_INVALID_ARG).  The call
- * allocates nothing.  Its first call on a device looks up that device's
- * address of the array (once per device, with the device current); make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race, so issue them on one stream. */
+ * allocates nothing.  The context's device must be the current device
+ * (otherwise GTC_ERR_INVALID_ARG).  Its first call on a device looks up that
+ * device's address of the array (once per device, with the device current);
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race, so issue them on one stream. */
 #define GTC_NOALLOC_MAX_KEYS 4194304u
 GTC_API gtc_status gtc_sort_pairs_u32_noalloc(gtc_ctx* ctx, uint32_t* keys, uint32_t* vals, uint32_t* keys_alt,
                                               uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,

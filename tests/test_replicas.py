@@ -27,6 +27,8 @@ def _rank(rank, world, port, out):
     try:
         ms = bench.max_over_ranks(pg, [3.0, 5.0][rank])
         units = bench.sum_over_ranks(pg, [100_000, 250_000][rank])
+        # an end-to-end loop each rank timed on its own (seconds per step)
+        e2e = bench.replica_rate(pg, [1_000_000, 1_000_000][rank], [0.002, 0.004][rank])
         pg.barrier()
         printed = ""
         if rank == 1:  # the reference arm stands down off rank 0, before any work
@@ -34,7 +36,7 @@ def _rank(rank, world, port, out):
             with contextlib.redirect_stdout(buf):
                 bench.run_reference(types.SimpleNamespace(n=10, steps=1, warmup=1, gpus=world))
             printed = buf.getvalue()
-        out.put((rank, ms, units, bench.job_rate(units, ms), printed))
+        out.put((rank, ms, units, bench.job_rate(units, ms), e2e, printed))
     finally:
         pg.destroy_process_group()
 
@@ -51,10 +53,11 @@ def test_two_gloo_replicas_combine_like_torchrun():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    for rank, ms, units, rate, printed in results:
+    for rank, ms, units, rate, e2e, printed in results:
         assert ms == 5.0  # the slowest rank's time
         assert units == 350_000  # every rank's units
         assert rate == pytest.approx(350_000 / 5e-3 / 1e6)
+        assert e2e == pytest.approx(2_000_000 / 0.004 / 1e6)  # both ranks' points over the slower loop
         assert printed == ""
 
 
@@ -65,3 +68,4 @@ def test_single_process_needs_no_group():
     assert bench.max_over_ranks(None, 2.5) == 2.5
     assert bench.sum_over_ranks(None, 7) == 7
     assert bench.job_rate(10_000_000, 0.8) == pytest.approx(12_500.0)
+    assert bench.replica_rate(None, 10_000_000, 0.002) == pytest.approx(5_000.0)
