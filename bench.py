@@ -10,6 +10,12 @@ build of that cloud.  Metric: Mpoints/s of the full build.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gtc|reference]
 
+The default line also carries `forms`: sort-only Mkeys/s of u32 and u64
+pairs at 2^24 keys, the learned-bucket form against the plain onesweep at
+2^26 keys, and the batched 512-cloud form, all measured in the same run, and
+the oracle's CPU build on all host threads and on one (`cpu_baseline`,
+`cpu_baseline_1t`).
+
 --impl reference times the CPU restatement of the reference's path (the
 oracle; the reference itself is Rust + Vulkan and cannot run here) on the
 host cores with all threads.  Under torchrun (N > 1) every rank builds its
@@ -50,9 +56,13 @@ def parse_args():
     ap.add_argument("--n", type=int, default=None,
                     help="points / keys (default: 10M for octree and sort, 64M (2^26) for learned)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["octree", "sort", "learned", "batched"], default="octree",
+    ap.add_argument("--no-forms", action="store_true",
+                    help="octree workload: skip the sort / learned / batched forms measured after the build")
+    ap.add_argument("--workload", choices=["octree", "sort", "learned", "batched", "cub_sort"], default="octree",
                     help="octree: the 10M clustered full build (default); sort: onesweep pairs sort only; "
-                         "learned: learned-bucket vs plain sort; batched: 512 clouds in one build")
+                         "learned: learned-bucket vs plain sort; batched: 512 clouds in one build; "
+                         "cub_sort: CUB's radix sort beside this project's on the same keys (bench-only)")
+    ap.add_argument("--begin-bit", type=int, default=0, help="cub_sort workload: first key bit sorted")
     ap.add_argument("--clouds", type=int, default=512, help="batched workload: number of clouds")
     ap.add_argument("--key-bits", type=int, default=64, help="sort workload: 32 or 64")
     ap.add_argument("--and-words", type=int, default=0, help="sort workload: AND of k uniform words (0 = uniform)")
@@ -204,6 +214,15 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+# ------------------------------------------------------------ config -------
+def octree_config(n):
+    """The workload's config object, the same in both arms (this project's
+    build and the reference arm), so that the two lines name one workload."""
+    return {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
+            "payload": "u32 point index",
+            "cloud": "32-component Gaussian mixture (sigma 0.5% of the domain) + 2% uniform noise, seed = rank"}
+
+
 # ------------------------------------------------------------ reference ---
 def run_reference(args):
     rank, world, _ = dist_info()
@@ -238,11 +257,229 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_points": args.n, "key_bits": KEY_BITS, "sample_points": ns},
+        "config": octree_config(args.n),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "details": {"sample_points": ns,
+                    "what": "the oracle (C++ restatement of the reference's shaders, pinned to them; the "
+                            "reference's Rust/Vulkan host cannot run here) on all host threads"},
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(pts_np, threads, budget_s=10.0, max_reps=8):
+    """The oracle's full build timed on the host cores (a bounded sample)."""
+    import numpy as np
+
+    import oracle
+
+    oracle.build()
+    n_all = pts_np.shape[0]
+    # Single-threaded builds of 10M points take seconds each: use a prefix.
+    ns = n_all if threads > 1 else min(n_all, 2_000_000)
+    sample = np.ascontiguousarray(pts_np[:ns])
+    reps = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.build_octree(sample, KEY_BITS, threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or reps >= max_reps:
+            break
+    what = "the same" if ns == n_all else f"the first {ns} points of the"
+    return {"value": round(ns * reps / el / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} full builds of {what} {n_all}-point cloud with the oracle ({threads} thread"
+                      f"{'s' if threads > 1 else ''})"}
+
+
+# --------------------------------------------------------- measurements ---
+def events_ms(stream, fn, reps, before=None):
+    """Mean CUDA-event time of fn() on `stream` over reps calls; before()
+    (untimed, e.g. restoring an unsorted input) runs ahead of each call."""
+    import torch
+
+    total = 0.0
+    for _ in range(reps):
+        if before:
+            before()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / reps
+
+
+def sort_keys(n, kb, and_words=0):
+    from gtc import workloads as W
+
+    return W.config3_keys(n, kb, and_words=and_words, seed=1)
+
+
+def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
+    """Stable onesweep sort of (key, u32 index) pairs, bits [0, kb).  Returns
+    timing, per-pass roofline and a sortedness / stable-permutation check."""
+    import numpy as np
+    import torch
+
+    import gtc
+
+    keys_np = sort_keys(n, kb, and_words)
+    kd = np.int32 if kb == 32 else np.int64
+    src_k = torch.from_numpy(keys_np.view(kd)).cuda()
+    src_v = torch.arange(n, dtype=torch.int32, device="cuda")
+    if variant is not None:
+        ctx.set_sort_variant(kb, variant)
+    ws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
+    k, v = torch.empty_like(src_k), torch.empty_like(src_v)
+    ka, va = torch.empty_like(src_k), torch.empty_like(src_v)
+    stream = torch.cuda.current_stream()
+
+    def restore():
+        k.copy_(src_k)
+        v.copy_(src_v)
+
+    def step():
+        ctx.sort_pairs(k, v, 0, kb, ws=ws, keys_alt=ka, vals_alt=va)
+
+    for _ in range(max(warmup, 3)):
+        restore()
+        step()
+    torch.cuda.synchronize()
+    ctx.device_status()
+    ctx.set_profiling(True)
+    ctx.stage_times(reset=True)
+    ms = events_ms(stream, step, steps, restore)
+    stages = ctx.stage_times(reset=True)
+    ctx.set_profiling(False)
+    ctx.device_status()
+    kk = k.cpu().numpy().view(keys_np.dtype)
+    vv = v.cpu().numpy().view(np.uint32)
+    ok = bool(np.all(kk[1:] >= kk[:-1])) and bool(np.array_equal(keys_np[vv], kk))
+    passes = kb // 8
+    K = kb // 8
+    os_ms, os_n = stages["onesweep"]
+    avg = os_ms / max(os_n, 1)
+    pass_bytes = 2 * (K + 4) * n
+    peak, _ = measured_hbm_peak()
+    return {"mkeys_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4), "n": n, "passes": passes,
+            "pass_ms": round(avg, 5), "pass_hbm_frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
+            "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4),
+            "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
+            "sort_variant": ctx.get_sort_variant(kb), "sorted_ok": ok}, stages
+
+
+def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
+    """Learned-bucket sort vs the plain onesweep on the learned workload's
+    64-bit Morton keys; the model trained on a 1% sample of a prior run's
+    sorted keys.  Both outputs are compared; a shifted mixture must fall back
+    and stay exact."""
+    import torch
+
+    import gtc
+    from gtc import workloads as W
+
+    def keys_of(seed, shifted=False, count=n):
+        pts = torch.from_numpy(W.config5_points(count, seed=seed, shifted=shifted)).cuda()
+        k, _ = ctx.morton(pts, 64, with_idx=False)
+        del pts
+        return k
+
+    stream = torch.cuda.current_stream()
+    prior = keys_of(1)
+    ctx.sort_pairs(prior, None, 0, 64)  # the pipeline's own previous sort
+    B = gtc.learned_buckets_for(n)
+    model = gtc.LearnedModel(ctx, B)
+    t0 = time.perf_counter()
+    loss = model.train(prior, stride=100, iters=100, lr=1e-4)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del prior
+    keys = keys_of(2)
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    ko, vo = torch.empty_like(keys), torch.empty_like(vals)
+    ws = ctx.workspace(gtc.OP_LEARNED_SORT, n, 64)
+    wk, wv = torch.empty_like(keys), torch.empty_like(vals)
+    ka, va = torch.empty_like(keys), torch.empty_like(vals)
+    sws = ctx.workspace(gtc.OP_SORT_PAIRS, n, 64)
+    flags = []
+
+    def learned_step():
+        flags.append(model.sort(keys, vals, ws=ws, keys_out=ko, vals_out=vo)[2])
+
+    def plain_step():
+        ctx.sort_pairs(wk, wv, 0, 64, ws=sws, keys_alt=ka, vals_alt=va)
+
+    def restore():
+        wk.copy_(keys)
+        wv.copy_(vals)
+
+    for _ in range(max(warmup, 3)):
+        learned_step()
+        restore()
+        plain_step()
+    torch.cuda.synchronize()
+    flags.clear()
+    learned_ms = events_ms(stream, learned_step, steps)
+    plain_ms = events_ms(stream, plain_step, steps, restore)
+    fl = max(int(f.item()) for f in flags)
+    identical = bool(torch.equal(ko, wk) and torch.equal(vo, wv))
+    ctx.device_status()
+    del wk, wv, ka, va, sws
+    shifted = keys_of(3, shifted=True, count=min(n, shifted_n))
+    sko, svo, sflags = model.sort(shifted)
+    sk2, sv2 = shifted.clone(), torch.arange(shifted.numel(), dtype=torch.int32, device="cuda")
+    ctx.sort_pairs(sk2, sv2, 0, 64)
+    shifted_ok = bool(torch.equal(sko, sk2) and torch.equal(svo, sv2))
+    counts = model.histogram(keys).cpu()
+    out = {"learned_mkeys_s": round(n / (learned_ms * 1e-3) / 1e6, 1), "learned_ms": round(learned_ms, 4),
+           "plain_mkeys_s": round(n / (plain_ms * 1e-3) / 1e6, 1), "plain_ms": round(plain_ms, 4),
+           "speedup_vs_plain": round(plain_ms / learned_ms, 3), "identical": identical, "flags": fl, "n": n,
+           "buckets": B, "train_loss": loss, "train_s": round(train_s, 3),
+           "bucket_max_over_mean": round(float(counts.max()) / (n / B), 3),
+           "shifted_n": int(shifted.numel()), "shifted_flags": int(sflags.item()), "shifted_exact": shifted_ok}
+    model.close()
+    return out
+
+
+def measure_batched(ctx, S, steps, warmup, seed=0, pts_np=None, offs_np=None):
+    """The batched build of S clouds (config-4 sizes and shapes) as one
+    CUDA-graph replay per step, plus an eager pass with per-stage events."""
+    import numpy as np
+    import torch
+
+    import gtc
+    from gtc import workloads as W
+
+    if pts_np is None:
+        pts_np, offs_np = W.config4_clouds(S, seed=seed)
+    n = pts_np.shape[0]
+    pts = torch.from_numpy(pts_np).cuda()
+    offs = torch.from_numpy(offs_np.view(np.int32)).cuda()
+    plan = gtc.BatchPlan(ctx, n, S, nodes_capacity=n + (n >> 1) + S)
+    for _ in range(max(warmup, 3)):
+        plan.launch(pts, offs)
+    torch.cuda.synchronize()
+    ctx.device_status()
+    ko, no, cc = plan.host_offsets()
+    u, o = int(ko[S]), int(no[S])
+    m = int(cc[:, 1].sum())
+    stream = torch.cuda.current_stream()
+    ctx.set_profiling(True)
+    ctx.stage_times(reset=True)
+    eager_ms = events_ms(stream, lambda: plan.launch(pts, offs), steps)
+    stages = ctx.stage_times(reset=True)
+    ctx.set_profiling(False)
+    ctx.device_status()
+    plan.capture(pts, offs)
+    for _ in range(3):
+        plan.replay()
+    torch.cuda.synchronize()
+    graph_ms = events_ms(stream, plan.replay, steps)
+    ctx.device_status()
+    return dict(plan=plan, pts=pts, offs=offs, pts_np=pts_np, offs_np=offs_np, n=n, u=u, m=m, o=o,
+                eager_ms=eager_ms, graph_ms=graph_ms, stages=stages)
 
 
 # ----------------------------------------------------------------- gtc ----
@@ -257,12 +494,11 @@ def run_gtc(args):
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    dev = f"cuda:{local}"
     pg = init_replicas(world)
 
     n = args.n
     pts_np = W.config2_points(n, seed=rank)
-    pts = torch.from_numpy(pts_np).to(dev)
+    pts = torch.from_numpy(pts_np).to(f"cuda:{local}")
     ctx = gtc.Context(local)
     # Autotune the onesweep shape on this workload's own Morton codes (the
     # pipeline's sort: 63 bits of 64-bit keys); the choice is cached per
@@ -291,13 +527,7 @@ def run_gtc(args):
     stream = torch.cuda.current_stream()
     ctx.set_profiling(True)
     ctx.stage_times(reset=True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        plan.launch(pts)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    eager_ms = e0.elapsed_time(e1) / args.steps
+    eager_ms = events_ms(stream, lambda: plan.launch(pts), args.steps)
     stages = ctx.stage_times(reset=True)
     ctx.set_profiling(False)
     ctx.device_status()
@@ -322,7 +552,6 @@ def run_gtc(args):
     clocks = clk.summary()
     ctx.device_status()
     elapsed_ms = max_over_ranks(pg, elapsed_ms)
-    graph_ms = elapsed_ms / args.steps
 
     # --- end to end through the host-buffer entry point (pinned host memory)
     L = ctx.L
@@ -399,17 +628,17 @@ def run_gtc(args):
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
-                   "onesweep_passes": 5, "sort_bits": "23..62, then the run fixup over bits 0..22", "payload": "u32 point index", "n_unique": u, "n_brt_nodes": m,
-                   "n_oct_nodes": o, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (160 MB of points, ~1 GB working set per build)",
-                   "timing": "CUDA-graph replay of the whole build per step",
-                   "eager_ms_per_step": round(eager_ms, 4), "stage_ms_per_step": stage_ms,
-                   "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
-                   "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
-                   "sort_variant": (args.sort_variant if args.sort_variant is not None
-                                    else gtc.autotune_lookup(KEY_BITS, 63 - SORT_BEGIN_BIT, n)),
-                   "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
+        "config": octree_config(n),
+        "details": {"onesweep_passes": 5, "sort_bits": "23..62, then the run fixup over bits 0..22",
+                    "n_unique": u, "n_brt_nodes": m, "n_oct_nodes": o, "parallelism": f"replicas{world}",
+                    "l2": "inputs larger than L2 (160 MB of points, ~1 GB working set per build)",
+                    "timing": "CUDA-graph replay of the whole build per step",
+                    "eager_ms_per_step": round(eager_ms, 4), "stage_ms_per_step": stage_ms,
+                    "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
+                    "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
+                    "sort_variant": (args.sort_variant if args.sort_variant is not None
+                                     else gtc.autotune_lookup(KEY_BITS, 63 - SORT_BEGIN_BIT, n)),
+                    "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
@@ -423,98 +652,170 @@ def run_gtc(args):
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
     }
+    del plan, pts
+    torch.cuda.empty_cache()
+    if not args.no_forms:
+        line["forms"] = measure_forms(ctx, args)
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(pts_np)
+        line["cpu_baseline"] = cpu_baseline(pts_np, cpu_threads())
+        line["cpu_baseline_1t"] = cpu_baseline(pts_np, 1)
     print(json.dumps(line), flush=True)
     ctx.close()
 
 
-def cpu_baseline(pts_np):
-    import oracle
+def measure_forms(ctx, args):
+    """The rest of the metric, measured in the same run on the same GPU:
+    sort-only Mkeys/s of u32 and u64 pairs at 2^24 keys (uniform), the
+    learned-bucket form against the plain onesweep at 2^26 keys, and the
+    batched form over 512 clouds."""
+    import torch
 
-    oracle.build()
-    threads = cpu_threads()
-    reps = 0
-    t0 = time.perf_counter()
-    while True:
-        oracle.build_octree(pts_np, KEY_BITS, threads=threads)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= 10.0 or reps >= 8:
-            break
-    n = pts_np.shape[0]
-    return {"value": round(n * reps / el / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{reps} full builds of the same {n}-point cloud with the oracle ({threads} threads)"}
+    steps = max(3, min(args.steps, 20))
+    forms = {}
+    for kb in (32, 64):
+        forms[f"sort_u{kb}_2p24"], _ = measure_sort(ctx, kb, 1 << 24, steps, 3)
+        torch.cuda.empty_cache()
+    forms["learned_vs_plain_2p26"] = measure_learned(ctx, LEARNED_KEYS, steps, 3)
+    torch.cuda.empty_cache()
+    b = measure_batched(ctx, 512, steps, 3)
+    forms["batched_512_clouds"] = {
+        "mpoints_s": round(b["n"] / (b["graph_ms"] * 1e-3) / 1e6, 1), "ms": round(b["graph_ms"], 4),
+        "n_points": b["n"], "eager_ms": round(b["eager_ms"], 4),
+        "stage_ms": {k: round(v[0] / steps, 4) for k, v in b["stages"].items() if v[1]}}
+    del b
+    torch.cuda.empty_cache()
+    return forms
 
 
 def run_gtc_sort(args):
     """Sort-only workload: stable onesweep sort of (key, u32 index) pairs."""
+    import gtc
+
+    kb, n = args.key_bits, args.n
+    ctx = gtc.Context(0)
+    with ClockSampler(0) as clk:
+        r, _ = measure_sort(ctx, kb, n, args.steps, args.warmup, args.and_words, args.sort_variant)
+    peak, peak_kind = measured_hbm_peak()
+    K = kb // 8
+    line = {
+        "metric": "Mkeys/s sort", "value": r["mkeys_s"], "unit": "Mkeys/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
+        "config": {"workload": f"sort_pairs_u{kb}_n{n}_and{args.and_words}", "n": n, "key_bits": kb},
+        "details": r,
+        "roofline": {"bound": "hbm", "kernel": "onesweep pass",
+                     "achieved": round(2 * (K + 4) * n / (r["pass_ms"] * 1e-3) / 1e9, 1), "peak": peak,
+                     "unit": "GB/s", "frac": r["pass_hbm_frac"], "traffic": None, "peak_kind": peak_kind,
+                     "avg_launch_ms": r["pass_ms"]},
+        "gpu_launches": (1 + r["passes"]) * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def cub_library():
+    """Builds (once) and loads bench-only libcubref.so: CUB's
+    DeviceRadixSort::SortPairs behind a C ABI, the comparison point of the
+    cub_sort workload.  Never part of libgtc.so."""
+    import ctypes
+
+    from gtc import _build
+
+    src = os.path.join(_build.PKG_ROOT, "bench", "cub_sort.cu")
+    out = os.path.join(_build.BUILD_DIR, "libcubref.so")
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        os.makedirs(_build.BUILD_DIR, exist_ok=True)
+        cmd = [_build._nvcc(), *_build.ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+               src, "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("libcubref build failed:\n" + r.stdout + r.stderr)
+    L = ctypes.CDLL(out)
+    P = ctypes.c_void_p
+    L.cubref_ws_bytes.argtypes = [ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+    L.cubref_sort_pairs.argtypes = [P, P, P, P, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
+                                    ctypes.c_size_t, P, ctypes.POINTER(ctypes.c_int)]
+    return L
+
+
+def run_cub_sort(args):
+    """CUB's onesweep (cub::DeviceRadixSort::SortPairs) beside this project's
+    sort on the same keys, bit range and GPU: the reference point for the
+    onesweep pass's roofline fraction.  --begin-bit picks the bit range
+    (23 = the pipeline's 64-bit sort over bits 23..62)."""
+    import ctypes
+
     import numpy as np
     import torch
 
     import gtc
-    from gtc import workloads as W
 
     kb, n = args.key_bits, args.n
-    keys_np = W.config3_keys(n, kb, and_words=args.and_words, seed=1)
+    end = 63 if (kb == 64 and args.begin_bit > 0) else kb
+    L = cub_library()
+    keys_np = sort_keys(n, kb, args.and_words)
     kd = np.int32 if kb == 32 else np.int64
     src_k = torch.from_numpy(keys_np.view(kd)).cuda()
     src_v = torch.arange(n, dtype=torch.int32, device="cuda")
-    ctx = gtc.Context(0)
-    if args.sort_variant is not None:
-        ctx.set_sort_variant(kb, args.sort_variant)
-    ws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
     k, v = torch.empty_like(src_k), torch.empty_like(src_v)
     ka, va = torch.empty_like(src_k), torch.empty_like(src_v)
+    b = ctypes.c_size_t()
+    assert L.cubref_ws_bytes(n, kb, ctypes.byref(b)) == 0
+    ws = torch.empty(max(b.value, 256), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
+    sel = ctypes.c_int()
 
-    def step():
-        ctx.sort_pairs(k, v, 0, kb, ws=ws, keys_alt=ka, vals_alt=va)
-
-    for _ in range(max(args.warmup, 3)):
+    def restore():
         k.copy_(src_k)
         v.copy_(src_v)
-        step()
+
+    def cub_step():
+        assert L.cubref_sort_pairs(k.data_ptr(), v.data_ptr(), ka.data_ptr(), va.data_ptr(), n, kb, args.begin_bit,
+                                   end, ws.data_ptr(), ws.numel(), stream.cuda_stream, ctypes.byref(sel)) == 0
+
+    for _ in range(max(args.warmup, 3)):
+        restore()
+        cub_step()
     torch.cuda.synchronize()
-    ctx.device_status()
+    with ClockSampler(0) as clk:
+        cub_ms = events_ms(stream, cub_step, args.steps, restore)
+    got_k = (ka if sel.value else k).clone()
+    got_v = (va if sel.value else v).clone()
+    ctx = gtc.Context(0)
+    gws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
+
+    def gtc_step():
+        ctx.sort_pairs(k, v, args.begin_bit, end, ws=gws, keys_alt=ka, vals_alt=va)
+
+    for _ in range(max(args.warmup, 3)):
+        restore()
+        gtc_step()
+    torch.cuda.synchronize()
     ctx.set_profiling(True)
     ctx.stage_times(reset=True)
-    total = 0.0
-    with ClockSampler(0) as clk:
-        for _ in range(args.steps):
-            k.copy_(src_k)  # restore the unsorted input outside the timed span
-            v.copy_(src_v)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            e1.synchronize()
-            total += e0.elapsed_time(e1)
+    gtc_ms = events_ms(stream, gtc_step, args.steps, restore)
     stages = ctx.stage_times(reset=True)
-    ctx.device_status()
-    # correctness of the last step: sorted, and the values are a stable permutation
-    kk = k.cpu().numpy().view(np.uint32 if kb == 32 else np.uint64)
-    vv = v.cpu().numpy().view(np.uint32)
-    ok = bool(np.all(kk[1:] >= kk[:-1])) and bool(np.array_equal(keys_np[vv], kk))
-    ms = total / args.steps
-    passes = kb // 8
-    os_ms, os_n = stages["onesweep"]
-    avg = os_ms / max(os_n, 1)
+    ctx.set_profiling(False)
+    identical = bool(torch.equal(k, got_k) and torch.equal(v, got_v))
+    passes = (end - args.begin_bit + 7) // 8
     K = kb // 8
-    pass_bytes = 2 * (K + 4) * n
     peak, peak_kind = measured_hbm_peak()
+    pass_bytes = 2 * (K + 4) * n
+    os_ms, os_n = stages["onesweep"]
     line = {
-        "metric": "Mkeys/s sort", "value": round(n / (ms * 1e-3) / 1e6, 2), "unit": "Mkeys/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
-        "config": {"workload": f"sort_pairs_u{kb}_n{n}_and{args.and_words}", "passes": passes,
-                   "sort_variant": ctx.get_sort_variant(kb), "variants": ctx.sort_variants(), "sorted_ok": ok,
-                   "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
-                   "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4)},
-        "roofline": {"bound": "hbm", "kernel": "onesweep pass", "achieved": round(pass_bytes / (avg * 1e-3) / 1e9, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
-                     "traffic": None, "peak_kind": peak_kind, "avg_launch_ms": round(avg, 5)},
-        "gpu_launches": (1 + passes) * args.steps,
+        "metric": "Mkeys/s sort (CUB comparison)", "value": round(n / (cub_ms * 1e-3) / 1e6, 1), "unit": "Mkeys/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cub_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
+        "config": {"workload": f"cub_sort_pairs_u{kb}_n{n}_bits{args.begin_bit}_{end}", "n": n, "key_bits": kb},
+        "details": {"impl": "cub::DeviceRadixSort::SortPairs (bench-only comparison)", "passes": passes,
+                    "cub_ms": round(cub_ms, 4), "cub_ms_per_pass": round(cub_ms / passes, 5),
+                    "gtc_ms": round(gtc_ms, 4), "gtc_pass_ms": round(os_ms / max(os_n, 1), 5),
+                    "gtc_hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 5),
+                    "gtc_over_cub": round(cub_ms / gtc_ms, 3), "identical_output": identical,
+                    "cub_pass_hbm_frac_upper": round(pass_bytes / (cub_ms / passes * 1e-3) / 1e9 / peak, 4),
+                    "gtc_pass_hbm_frac": round(pass_bytes / (os_ms / max(os_n, 1) * 1e-3) / 1e9 / peak, 4)},
+        "gpu_launches": None,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -527,106 +828,30 @@ def run_gtc_learned(args):
     weights, 5% noise).  The model is trained on a 1% sample of a prior run's
     sorted keys (same mixture, another seed); both sorts must give identical
     output; a shifted mixture must take the onesweep fallback."""
-    import numpy as np
-    import torch
-
     import gtc
-    from gtc import workloads as W
 
     n = args.n
     ctx = gtc.Context(0)
-    stream = torch.cuda.current_stream()
-
-    def keys_of(seed, shifted=False, count=n):
-        pts = torch.from_numpy(W.config5_points(count, seed=seed, shifted=shifted)).cuda()
-        k, _ = ctx.morton(pts, 64, with_idx=False)
-        del pts
-        return k
-
-    prior = keys_of(1)
-    ctx.sort_pairs(prior, None, 0, 64)  # the pipeline's own previous sort
-    B = gtc.learned_buckets_for(n)
-    model = gtc.LearnedModel(ctx, B)
-    t0 = time.perf_counter()
-    loss = model.train(prior, stride=100, iters=100, lr=1e-4)
-    train_s = time.perf_counter() - t0
-    del prior
-    keys = keys_of(2)
-    vals = torch.arange(n, dtype=torch.int32, device="cuda")
-    ko, vo = torch.empty_like(keys), torch.empty_like(vals)
-    ws = ctx.workspace(gtc.OP_LEARNED_SORT, n, 64)
-    flags = None
-    wk, wv = torch.empty_like(keys), torch.empty_like(vals)
-    ka, va = torch.empty_like(keys), torch.empty_like(vals)
-    sws = ctx.workspace(gtc.OP_SORT_PAIRS, n, 64)
-
-    def learned_step():
-        nonlocal flags
-        _, _, flags = model.sort(keys, vals, ws=ws, keys_out=ko, vals_out=vo)
-
-    def plain_step():
-        ctx.sort_pairs(wk, wv, 0, 64, ws=sws, keys_alt=ka, vals_alt=va)
-
-    def timed(step, restore=None):
-        for _ in range(max(args.warmup, 3)):
-            if restore:
-                restore()
-            step()
-        torch.cuda.synchronize()
-        total = 0.0
-        for _ in range(args.steps):
-            if restore:
-                restore()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            e1.synchronize()
-            total += e0.elapsed_time(e1)
-        return total / args.steps
-
-    def restore():
-        wk.copy_(keys)
-        wv.copy_(vals)
-
     with ClockSampler(0) as clk:
-        learned_ms = timed(learned_step)
-        plain_ms = timed(plain_step, restore)
-    fl = int(flags.item())
-    identical = bool(torch.equal(ko, wk) and torch.equal(vo, wv))
-    ctx.device_status()
-    # A distribution the model was not trained on must fall back, exactly.
-    shifted = keys_of(3, shifted=True, count=min(n, 8_000_000))
-    sko, svo, sflags = model.sort(shifted)
-    sk2, sv2 = shifted.clone(), torch.arange(shifted.numel(), dtype=torch.int32, device="cuda")
-    ctx.sort_pairs(sk2, sv2, 0, 64)
-    shifted_ok = bool(torch.equal(sko, sk2) and torch.equal(svo, sv2))
-    counts = model.histogram(keys).cpu().numpy()
-    top = torch.bincount((keys >> 52).to(torch.int64), minlength=4096).cpu().numpy()
+        r = measure_learned(ctx, n, args.steps, args.warmup)
     peak, peak_kind = measured_hbm_peak()
-    # compulsory bytes of the learned path per key: count read 8, scatter
-    # read 12 + write 16, bucket sort read 16 + write 12
-    lbytes = 64 * n
+    # compulsory bytes of the learned path per key: model read 8, bucket
+    # scatter read 12 + write 12, in-bucket sort read 12 + write 12
+    lbytes = 56 * n
     line = {
-        "metric": "Mkeys/s learned-bucket sort", "value": round(n / (learned_ms * 1e-3) / 1e6, 2), "unit": "Mkeys/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(learned_ms, 4),
+        "metric": "Mkeys/s learned-bucket sort", "value": r["learned_mkeys_s"], "unit": "Mkeys/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["learned_ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": f"learned_sort_u64_n{n}", "buckets": B, "train_loss": loss,
-                   "train_s": round(train_s, 3), "flags": fl, "identical_to_onesweep": identical,
-                   "plain_onesweep_mkeys_s": round(n / (plain_ms * 1e-3) / 1e6, 2),
-                   "plain_ms": round(plain_ms, 4), "speedup_vs_plain": round(plain_ms / learned_ms, 3),
-                   "shifted_flags": int(sflags.item()), "shifted_exact": shifted_ok,
-                   "bucket_max_over_mean": round(float(counts.max() / (n / B)), 3),
-                   "topbits_max_over_mean": round(float(top.max() / (n / 4096)), 3)},
-        "roofline": {"bound": "hbm", "kernel": "learned path (count + scatter + bucket sort)",
-                     "achieved": round(lbytes / (learned_ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(lbytes / (learned_ms * 1e-3) / 1e9 / peak, 4), "traffic": None,
+        "config": {"workload": f"learned_sort_u64_n{n}", "n": n, "key_bits": 64},
+        "details": r,
+        "roofline": {"bound": "hbm", "kernel": "learned path (model + bucket scatter + in-bucket sort)",
+                     "achieved": round(lbytes / (r["learned_ms"] * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(lbytes / (r["learned_ms"] * 1e-3) / 1e9 / peak, 4), "traffic": None,
                      "peak_kind": peak_kind},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": None,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
-    model.close()
     ctx.close()
 
 
@@ -646,37 +871,12 @@ def run_gtc_batched(args):
     pg = init_replicas(world)
     S = args.clouds
     pts_np, offs_np = W.config4_clouds(S, seed=rank)
-    n = pts_np.shape[0]
-    pts = torch.from_numpy(pts_np).cuda()
-    offs = torch.from_numpy(offs_np.view(np.int32)).cuda()
     ctx = gtc.Context(local)
-    plan = gtc.BatchPlan(ctx, n, S, nodes_capacity=n + (n >> 1) + S)
-    for _ in range(max(args.warmup, 3)):
-        plan.launch(pts, offs)
-    torch.cuda.synchronize()
-    ctx.device_status()
-    ko, no, cc = plan.host_offsets()
-    u, o = int(ko[S]), int(no[S])
-    m = int(cc[:, 1].sum())
-    # Per-stage breakdown: eager builds with CUDA events around every stage.
+    b = measure_batched(ctx, S, 3, args.warmup, pts_np=pts_np, offs_np=offs_np)
+    plan, pts, offs, n, u, m, o = b["plan"], b["pts"], b["offs"], b["n"], b["u"], b["m"], b["o"]
+    stages = b["stages"]
     stream = torch.cuda.current_stream()
-    ctx.set_profiling(True)
-    ctx.stage_times(reset=True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        plan.launch(pts, offs)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    eager_ms = e0.elapsed_time(e1) / args.steps
-    stages = ctx.stage_times(reset=True)
-    ctx.set_profiling(False)
-    ctx.device_status()
     # Timed region: one CUDA-graph replay of the whole batch per step.
-    plan.capture(pts, offs)
-    for _ in range(3):
-        plan.replay()
-    torch.cuda.synchronize()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         if pg:
@@ -694,7 +894,6 @@ def run_gtc_batched(args):
     ctx.device_status()
     elapsed_ms = max_over_ranks(pg, elapsed_ms)
     n_job = sum_over_ranks(pg, n)  # the ranks' clouds differ (seed = rank)
-    graph_ms = elapsed_ms / args.steps
 
     # End to end: pinned host points in, every cloud's octree nodes out.
     hp = torch.empty_like(pts, device="cpu").pin_memory()
@@ -720,20 +919,20 @@ def run_gtc_batched(args):
     peak, peak_kind = measured_hbm_peak()
     alg_total = sum(algorithmic_bytes(n, u, m, o, 4).values())
     ms_per_step = elapsed_ms / args.steps
-    stage_ms = {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1]}
+    stage_ms = {k: round(v[0] / 3, 4) for k, v in stages.items() if v[1]}
     sizes = np.diff(offs_np.astype(np.int64))
     line = {
         "metric": "Mpoints/s batched octree build", "value": round(job_rate(n_job, ms_per_step), 2),
         "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"batched_{S}_clouds_u32", "n_clouds": S, "n_points": n,
-                   "cloud_min": int(sizes.min()), "cloud_max": int(sizes.max()), "n_unique": u, "n_oct_nodes": o,
-                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (points alone exceed 1 GB)",
-                   "timing": "CUDA-graph replay of the whole batch per step",
-                   "eager_ms_per_step": round(eager_ms, 4), "stage_ms_per_step": stage_ms,
-                   "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
-                   "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4)},
+        "config": {"workload": f"batched_{S}_clouds_u32", "n_clouds": S, "n_points": n},
+        "details": {"cloud_min": int(sizes.min()), "cloud_max": int(sizes.max()), "n_unique": u, "n_oct_nodes": o,
+                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (points alone exceed 1 GB)",
+                    "timing": "CUDA-graph replay of the whole batch per step",
+                    "eager_ms_per_step": round(b["eager_ms"], 4), "stage_ms_per_step": stage_ms,
+                    "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
+                    "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4)},
         "roofline": {"bound": "hbm", "kernel": "bt_onesweep_kernel (one segmented 8-bit pass, u32 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": None, "peak_kind": peak_kind, "bytes_per_launch": pass_bytes,
@@ -753,6 +952,8 @@ def main():
         args.n = LEARNED_KEYS if args.workload == "learned" else N_POINTS
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "cub_sort":
+        run_cub_sort(args)
     elif args.workload == "sort":
         run_gtc_sort(args)
     elif args.workload == "learned":

@@ -117,6 +117,7 @@ struct gtc_ctx {
   QueuedOut qout[NQ];
   gtc_status qerr = GTC_OK;  // first host-side error of a queued build, reported by the wait
   int qnext = 0;
+  bool skip_first_tile = false;  // gtc_debug_skip_first_tile: one-shot, consumed by the next sort
 };
 
 namespace {
@@ -245,6 +246,16 @@ gtc_status sort_pairs_impl(gtc_ctx* ctx, K* keys, uint32_t* vals, K* keys_alt, u
   const Launch L = launch_of(ctx, stream);
   const SortWorkspace Wk = carve_sort_workspace(ws, n, passes, 0);
   GTC_TRY(ctx, cudaMemsetAsync(Wk.header, 0, Wk.header_words * 4, S(stream)));
+  if (ctx->skip_first_tile) {
+    // The LAST pass's tile tickets start at 1 (header word 1 + p is pass p's
+    // counter; byte 0 of the little-endian word): its tile 0 is never sorted
+    // or published.  The last pass reads input whose digit counts match the
+    // global histogram, so a tile's writes for digit d land in
+    // [bin_off[d] + excl, bin_off[d] + excl + count) and a timed-out look-back
+    // only makes excl smaller (the passes also check every write index).
+    ctx->skip_first_tile = false;
+    GTC_TRY(ctx, cudaMemsetAsync(Wk.header + passes, 1, 1, S(stream)));
+  }
   {
     StageTimer t(ctx, stream, GTC_STAGE_HISTOGRAM);
     GTC_TRY(ctx, launch_global_hist<K>(L, keys, n, begin_bit, end_bit, Wk, passes));
@@ -570,6 +581,18 @@ GTC_API gtc_status gtc_device_status(gtc_ctx* ctx, gtc_stream_t stream) {
   if (word & DEV_CAPACITY) return fail(ctx, GTC_ERR_CAPACITY, "octree node buffer too small");
   if (word & DEV_BAD_INPUT) return fail(ctx, GTC_ERR_INVALID_ARG, "device-resident offsets are not a valid partition");
   if (word & DEV_INTERNAL) return fail(ctx, GTC_ERR_CUDA, "device consistency check failed");
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_set_spin_limit(gtc_ctx* ctx, uint32_t polls) {
+  GTC_ARG(ctx, ctx, "null context");
+  GTC_TRY(ctx, cudaMemcpy(ctx->d_status + 1, &polls, 4, cudaMemcpyHostToDevice));
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_debug_skip_first_tile(gtc_ctx* ctx) {
+  GTC_ARG(ctx, ctx, "null context");
+  ctx->skip_first_tile = true;
   return GTC_OK;
 }
 

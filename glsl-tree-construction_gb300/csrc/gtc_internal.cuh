@@ -23,8 +23,9 @@ constexpr uint32_t FLAG_NOT_READY = 0u;
 constexpr uint32_t FLAG_AGGREGATE = 1u;
 constexpr uint32_t FLAG_INCLUSIVE = 2u;
 
-// Spins poll at most this many times (with __nanosleep backoff after the
-// first few), i.e. well under a second, before giving up with DEV_TIMEOUT.
+// Default poll budget of a bounded spin (with __nanosleep backoff after the
+// first few polls), well under a second, before it gives up with DEV_TIMEOUT.
+// gtc_set_spin_limit replaces it per context.
 constexpr uint32_t SPIN_LIMIT = 1u << 20;
 
 constexpr int NUM_SMS_GB300 = 152;
@@ -106,14 +107,24 @@ __device__ __forceinline__ void st_hint(uint64_t* p, uint64_t v, uint64_t pol) {
 // Hint: fetch the 128-byte line holding p into L2.
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-// Waits until *p carries a flag, at most SPIN_LIMIT polls.  On expiry records
-// DEV_TIMEOUT and returns an INCLUSIVE descriptor of value 0 so the caller's
-// look-back ends.
+// Poll budget of the bounded waits: word 1 of the context's status buffer
+// when nonzero (gtc_set_spin_limit), else SPIN_LIMIT.  Read only once a wait
+// has actually started.
+__device__ __forceinline__ uint32_t spin_budget(const uint32_t* status) {
+  const uint32_t b = ld_relaxed(status + 1);
+  return b ? b : SPIN_LIMIT;
+}
+
+// Waits until *p carries a flag, at most spin_budget() polls.  On expiry
+// records DEV_TIMEOUT and returns an INCLUSIVE descriptor of value 0 so the
+// caller's look-back ends.
 __device__ __forceinline__ uint32_t spin_descriptor(const uint32_t* p, uint32_t* status) {
   uint32_t v = ld_relaxed(p);
+  if ((v & 3u) != FLAG_NOT_READY) return v;
+  const uint32_t limit = spin_budget(status);
   uint32_t it = 0;
   while ((v & 3u) == FLAG_NOT_READY) {
-    if (++it > SPIN_LIMIT) {
+    if (++it > limit) {
       atomicOr(status, DEV_TIMEOUT);
       return FLAG_INCLUSIVE;
     }
@@ -182,7 +193,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait for the phase with the given parity to complete.  Returns
 // false (and records DEV_TIMEOUT) if the copy never lands.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t* status) {
-  for (uint32_t it = 0; it < SPIN_LIMIT; ++it) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint32_t limit = spin_budget(status);
+  for (uint32_t it = 0; it < limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 16) __nanosleep(32);
   }

@@ -523,6 +523,9 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   }
   __syncthreads();
   const uint32_t tile = s.tile_id;
+  // A ticket past the last tile has nothing to sort (tickets start at 0, so
+  // only a counter advanced on purpose, gtc_debug_skip_first_tile, gets here).
+  if (tile >= (n + TILE - 1) / TILE) return;
   const uint32_t tile_base = tile * TILE;
 
   // 2. warp-striped coalesced loads.
@@ -653,11 +656,15 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   }
   __syncthreads();
 
-  // 7. coalesced writes of each digit run.
+  // 7. coalesced writes of each digit run.  o < n always holds while every
+  // look-back completes; after one ran out (DEV_TIMEOUT) a later pass may see
+  // digit counts that disagree with the global histogram, and the check keeps
+  // its writes in bounds.
   const uint32_t valid = min((uint32_t)TILE, n - tile_base);
   for (uint32_t i = tid; i < valid; i += THREADS) {
     const K k = s.keys[i];
     const uint32_t o = s.global_base[(uint32_t)(k >> shift) & dmask] + i;
+    if (o >= n) continue;
     if (L2H) {
       st_hint(kout + o, k, pol_out);
       if (HAS_VALS) st_hint(vout + o, s.vals[i], pol_out);
@@ -860,6 +867,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS <= 256 ? 2 : 1)) onesweep_tm
     for (uint32_t i = tid; i < valid; i += THREADS) {
       const K k = s.keys[buf][i];
       const uint32_t o = s.gbase[(uint32_t)(k >> shift) & dmask] + i;
+      if (o >= n) continue;  // only after a timed-out look-back (see onesweep_kernel)
       kout[o] = k;
       if (HV) vout[o] = s.vals[buf][i];
     }

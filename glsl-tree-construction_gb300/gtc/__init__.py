@@ -92,6 +92,15 @@ class Context:
     def device_status_code(self, stream=None) -> int:
         return self.L.gtc_device_status(self.h, _stream(stream))
 
+    def set_spin_limit(self, polls: int):
+        """Poll budget of this context's bounded device waits (0: the default)."""
+        self.check(self.L.gtc_set_spin_limit(self.h, polls))
+
+    def debug_skip_first_tile(self):
+        """The next sort_pairs hands out tile tickets from 1 (tile 0 never
+        publishes; its look-backs time out).  For tests of the timeout path."""
+        self.check(self.L.gtc_debug_skip_first_tile(self.h))
+
     def set_profiling(self, on: bool):
         self.check(self.L.gtc_set_profiling(self.h, 1 if on else 0))
 

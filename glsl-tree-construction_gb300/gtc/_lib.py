@@ -39,6 +39,8 @@ SIGNATURES = {
     "gtc_last_error": (ctypes.c_char_p, [P]),
     "gtc_device_status": (st, [P, P]),
     "gtc_version": (ctypes.c_char_p, []),
+    "gtc_set_spin_limit": (st, [P, u32]),
+    "gtc_debug_skip_first_tile": (st, [P]),
     "gtc_set_profiling": (st, [P, i_]),
     "gtc_stage_times": (st, [P, P, P, i_]),
     "gtc_workspace_size": (st, [P, i_, u32, i_, ctypes.POINTER(sz)]),

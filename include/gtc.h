@@ -77,6 +77,21 @@ GTC_API gtc_status gtc_device_status(gtc_ctx* ctx, gtc_stream_t stream);
 /* Library version string and the number of kernel variants compiled in. */
 GTC_API const char* gtc_version(void);
 
+/* Bounded device waits.  Every spin of a kernel on another block's result (the
+ * onesweep look-back, the resident segment scans, TMA copy completion) polls
+ * at most a budget of times and then records GTC_ERR_TIMEOUT in the status
+ * word and returns, so a lost predecessor never hangs the GPU; the reference's
+ * look-back spin is unbounded (new_radix_sort.comp:209-223).  The budget is
+ * 2^20 polls with backoff (well under a second); gtc_set_spin_limit sets it
+ * for this context (polls = 0 restores the default).  gtc_debug_skip_first_tile
+ * makes the next gtc_sort_pairs_u32/u64 on this context hand out its last
+ * pass's tile tickets from 1, so that pass's tile 0 is never sorted and never
+ * publishes its counts: the look-backs that reach it run out of polls (a test
+ * of the timeout path; that sort's output is then undefined but every write
+ * stays in bounds).  One-shot.  Neither has a counterpart in the reference. */
+GTC_API gtc_status gtc_set_spin_limit(gtc_ctx* ctx, uint32_t polls);
+GTC_API gtc_status gtc_debug_skip_first_tile(gtc_ctx* ctx);
+
 /* Record per-stage CUDA events around every launch (0 = off, the default). */
 GTC_API gtc_status gtc_set_profiling(gtc_ctx* ctx, int enable);
 /* Sum of event-timed milliseconds per stage since the last reset, and the

@@ -5,6 +5,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -77,3 +78,32 @@ def test_batched_workspace_and_args_without_device(gtc_mod):
     assert L.gtc_batched_workspace_size(1 << 30, 4, ctypes.byref(b)) == 1  # too many points
     assert L.gtc_batched_workspace_size(1000, (1 << 20) + 1, ctypes.byref(b)) == 1  # too many clouds
     assert L.gtc_build_octree_batched(None, None, None, 1, 0, 0.0, 1.0, None, None, 0, None) == 1
+
+
+def _spread3(v):
+    out = np.zeros_like(v, dtype=np.uint32)
+    for b in range(10):
+        out |= ((v >> np.uint32(b)) & np.uint32(1)) << np.uint32(3 * b)
+    return out
+
+
+def test_ref_morton32_to_xyz_host_decode(gtc_mod, oracle):
+    """gtc_ref_morton32_to_xyz (morton.rs:43-74, host code, no device): every
+    corner of the reference fixture's octree decodes back from its code, and
+    random codes under an odd min/range decode exactly as the oracle does
+    (separately rounded divide, multiply and add)."""
+    L = gtc_mod.lib()
+    fx = np.load(os.path.join(REPO, "tests", "golden", "ref_pipeline_32.npz"))
+    corners = fx["nodes"].view(np.float32)[:, 8:12]
+    q = corners[:, :3].astype(np.uint32)  # min 0, range 1024: a corner is its cell coordinate
+    assert np.array_equal(q.astype(np.float32), corners[:, :3])
+    codes = _spread3(q[:, 0]) | (_spread3(q[:, 1]) << np.uint32(1)) | (_spread3(q[:, 2]) << np.uint32(2))
+    out = np.zeros(4, np.float32)
+    for c, corner in zip(codes, corners):
+        L.gtc_ref_morton32_to_xyz(out.ctypes.data_as(ctypes.c_void_p), int(c), 0.0, 1024.0)
+        assert out.tobytes() == corner.tobytes()
+    rng = np.random.default_rng(5)
+    for c in rng.integers(0, 1 << 30, 2000, dtype=np.uint32):
+        for mn, rg in ((-3.7, 17.3), (0.1, 0.3), (100.0, 1024.0)):
+            L.gtc_ref_morton32_to_xyz(out.ctypes.data_as(ctypes.c_void_p), int(c), mn, rg)
+            assert out.tobytes() == oracle.morton_to_xyz(int(c), 32, mn, rg).tobytes()

@@ -132,3 +132,40 @@ def test_trained_model_gain_over_top_bits(ctx, oracle, gtc_mod):
     assert learned.max() / mean < 2.0
     assert top.max() / mean > 20.0
     assert (top.max() / mean) / (learned.max() / mean) > 10.0
+
+
+def test_config5_full_64m(ctx, gtc_mod):
+    """The learned-bucket workload at its stated size: 2^26 (64M) u64 Morton
+    keys of the 64-component mixture (sigma 0.3-3% of the domain, Dirichlet(1)
+    weights, 5% noise).  The model is trained on a 1% sample of a prior run's
+    sorted keys (the same mixture, another seed).  The output must be
+    byte-equal to the plain onesweep (gtc_sort_pairs_u64, stable, all 64
+    bits) without the fallback; the shifted mixture must set the fallback
+    flag and still come out byte-equal."""
+    import torch
+
+    n = 1 << 26
+
+    def keys_of(seed, shifted=False):
+        pts = torch.from_numpy(W.config5_points(n, seed=seed, shifted=shifted)).cuda()
+        k, _ = ctx.morton(pts, 64, with_idx=False)
+        del pts
+        return k
+
+    prior = keys_of(1)
+    ctx.sort_pairs(prior, None, 0, 64)
+    B = gtc_mod.learned_buckets_for(n)
+    model = gtc_mod.LearnedModel(ctx, B)
+    model.train(prior, stride=100, iters=100, lr=1e-4)
+    del prior
+    for seed, shifted in ((2, False), (3, True)):
+        keys = keys_of(seed, shifted)
+        ko, vo, flags = model.sort(keys)
+        k2, v2 = keys.clone(), torch.arange(n, dtype=torch.int32, device="cuda")
+        ctx.sort_pairs(k2, v2, 0, 64)
+        fl = int(flags.item())
+        assert (fl != 0) == shifted, (shifted, fl, gtc_mod.LEARNED_FLAGS)
+        assert torch.equal(ko, k2) and torch.equal(vo, v2)
+        ctx.device_status()
+        del keys, ko, vo, k2, v2
+    model.close()
