@@ -392,7 +392,7 @@ def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
     B = gtc.learned_buckets_for(n)
     model = gtc.LearnedModel(ctx, B)
     t0 = time.perf_counter()
-    loss = model.train(prior, stride=100, iters=100, lr=1e-4)
+    loss = model.train(prior, stride=100)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     del prior

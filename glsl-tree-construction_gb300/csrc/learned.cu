@@ -44,41 +44,28 @@ constexpr uint32_t LFLAG_OVERFLOW = 1u;   // a bucket exceeds the on-chip sort c
 constexpr uint32_t LFLAG_ORDER = 2u;      // bucket key ranges out of order
 constexpr uint32_t LFLAG_BAD_MODEL = 4u;  // heights not non-decreasing
 
-constexpr int LC_THREADS = 1024;
-constexpr int LC_KPT = 64;
-constexpr int LC_TILE = LC_THREADS * LC_KPT;  // 65536 keys per count/scatter tile
-constexpr int BS_THREADS = 1024;
-constexpr int BS_CAP = 16384;                 // keys per bucket sorted on chip (229,920 B of smem)
-constexpr int MAX_BUCKETS = 8192;  // knots + heights + histogram must fit one CTA's shared memory
+constexpr int LC_THREADS = 1024;  // count kernel: one resident CTA per SM, looping over the keys
+constexpr int LC_ILP = 4;          // keys per thread searched at once (independent dependency chains)
+constexpr int BS_THREADS = 512;    // in-bucket sort: two CTAs per SM
+constexpr int BS_CAP = 8192;       // keys per bucket sorted on chip
+constexpr int BS_IPT = BS_CAP / BS_THREADS;
+constexpr int MAX_BUCKETS = 16384;  // the Eytzinger knots + bucket histogram fill one CTA's shared memory
 
 // ---------------------------------------------------------------- model ---
-// The interior knots kn[1..B-1] (B a power of two: a perfect binary tree) are
-// also kept in breadth-first (Eytzinger) order e[1..B-1], so the lanes of a
-// warp that walk down the tree read consecutive words at every level instead
-// of striding through one shared-memory bank as a plain binary search over a
-// power-of-two array does.
-__device__ __forceinline__ void build_eytzinger(uint64_t* e, const uint64_t* kn, int B) {
-  const int d = 31 - __clz(B);
-  for (int i = threadIdx.x; i < B; i += blockDim.x) {
-    if (i == 0) continue;
-    const int L = 31 - __clz(i);
-    const int rank = ((2 * (i - (1 << L)) + 1) << (d - 1 - L)) - 1;  // in-order position
-    e[i] = kn[rank + 1];
-  }
-}
-
-__device__ __forceinline__ int model_bucket(uint64_t key, const uint64_t* e, const uint64_t* kn, const float* y,
-                                            int B) {
-  int i = 1;
-  while (i < B) i = 2 * i + (e[i] <= key ? 1 : 0);
-  const int lo = i - B;  // interior knots <= key == segment index (kn[0] == 0)
-  const uint64_t k0 = kn[lo], k1 = kn[lo + 1];
-  const float y0 = y[lo], y1 = y[lo + 1];
-  const float w = (k1 > k0) ? __fdiv_rn((float)(key - k0), (float)(k1 - k0)) : 0.0f;
-  float F = __fadd_rn(y0, __fmul_rn(__fsub_rn(y1, y0), w));
-  F = fminf(fmaxf(F, y0), y1);
-  const int b = __float2int_rz(__fmul_rn(F, (float)B));
-  return min(max(b, 0), B - 1);
+// Per-segment bucket line, derived from the heights before every sort:
+// t(key) = a + c * float(key - kn[s]) clamped to amax, with a = B * y[s],
+// amax = B * y[s + 1], c = B * (y[s + 1] - y[s]) / float(kn[s + 1] - kn[s]).
+// Every operation is one IEEE round-to-nearest step (no contraction), so the
+// oracle (orc_pwl_buckets) evaluates the same function bit for bit.  For
+// non-decreasing heights t is non-decreasing in the key: inside a segment
+// each rounding step is monotone and c >= 0; at a knot the segment's clamp
+// amax equals the next segment's start a.  bucket = floor(t) is therefore
+// monotone, which makes bucket key ranges ordered by construction.
+__device__ __forceinline__ int model_bucket(uint64_t key, int seg, const uint64_t* kn, const float4* segp, int B) {
+  const float4 p = __ldg(segp + seg);
+  const uint64_t k0 = __ldg(kn + seg);
+  const float t = fminf(__fadd_rn(p.x, __fmul_rn(p.y, __ull2float_rn(key - k0))), p.z);
+  return min(__float2int_rz(t), B - 1);
 }
 
 // Segment of a key and its interpolation weight (the training forward pass).
@@ -110,6 +97,10 @@ __global__ void sample_kernel(const uint64_t* sorted, uint32_t ns, uint32_t stri
     sample[j] = sorted[(size_t)j * stride];
 }
 
+// Knots at the sample's quantiles (fixed); heights initialised to the
+// uniform CDF over the key space, y = key / 2^64, i.e. equal-width buckets of
+// the key range: the model before training.  Training moves the heights to
+// the data's CDF.
 __global__ void knots_init_kernel(const uint64_t* sample, uint32_t ns, int B, uint64_t* kn, float* y, float* m1,
                                   float* m2) {
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= B; b += gridDim.x * blockDim.x) {
@@ -118,7 +109,7 @@ __global__ void knots_init_kernel(const uint64_t* sample, uint32_t ns, int B, ui
     else if (b == B) k = ~0ull;
     else k = sample[(uint64_t)b * ns / (uint32_t)B];
     kn[b] = k;
-    y[b] = (float)b / (float)B;
+    y[b] = (b == B) ? 1.0f : __ull2float_rn(k) * 0x1p-64f;
     m1[b] = 0.0f;
     m2[b] = 0.0f;
   }
@@ -218,37 +209,71 @@ constexpr int LP_KPT = 16;
 constexpr int LP_TILE = LP_THREADS * LP_KPT;  // 4096 keys per pass tile
 constexpr int LP_RADIX = 128;                 // bucket-id digits of at most 7 bits
 constexpr int LP_WARPS = LP_THREADS / 32;
-constexpr int BS_GROUP = 32;                  // longest equal-prefix group finished by insertion
 
-__device__ __forceinline__ void load_model(uint64_t* s_kn, float* s_y, const uint64_t* kn, const float* y, int B) {
-  for (int i = threadIdx.x; i <= B; i += blockDim.x) {
-    s_kn[i] = kn[i];
-    s_y[i] = y[i];
+// 0. model preparation before a sort (one thread per segment): the bucket
+// lines of model_bucket, the interior knots in Eytzinger order for the
+// count kernel's search, and the monotonicity check of the heights.
+__global__ void learned_prepare_kernel(const uint64_t* kn, const float* y, int B, uint64_t* eytz, float4* segp,
+                                       uint32_t* flags) {
+  const int d = 31 - __clz(B);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B; i += gridDim.x * blockDim.x) {
+    const float y0 = y[i], y1 = y[i + 1];
+    const uint64_t k0 = kn[i], k1 = kn[i + 1];
+    const float fb = (float)B;
+    const float dy = __fmul_rn(fb, __fsub_rn(y1, y0));
+    const float c = (k1 > k0 && dy > 0.0f) ? __fdiv_rn(dy, __ull2float_rn(k1 - k0)) : 0.0f;
+    segp[i] = make_float4(__fmul_rn(fb, y0), c, __fmul_rn(fb, y1), 0.0f);
+    if (flags && !(y0 <= y1)) atomicOr(flags, LFLAG_BAD_MODEL);
+    if (i > 0) {  // node i of the perfect tree over interior knots 1..B-1
+      const int L = 31 - __clz(i);
+      const int rank = ((2 * (i - (1 << L)) + 1) << (d - 1 - L)) - 1;  // in-order position
+      eytz[i] = kn[rank + 1];
+    }
   }
 }
 
-// 1. bucket of every key (written as u16 when bids is set) and the global
-// bucket histogram (one atomic per non-empty bucket and tile).
-__global__ void __launch_bounds__(LC_THREADS) learned_count_kernel(const uint64_t* __restrict__ keys, uint32_t n,
-                                                                   const uint64_t* kn, const float* y, int B,
-                                                                   uint32_t* totals, uint16_t* __restrict__ bids) {
+// 1. bucket of every key (written as u16 when bids is set) and the bucket
+// histogram.  One resident CTA per SM loops over the keys; the interior knots
+// sit in shared memory in Eytzinger (breadth-first) order, so the lanes of a
+// warp walking down the tree read neighbouring words at every level, and each
+// thread walks LC_ILP keys at once to keep several shared-memory loads in
+// flight.  The segment's bucket line then comes from global memory (L1/L2).
+__global__ void __launch_bounds__(LC_THREADS, 1) learned_count_kernel(const uint64_t* __restrict__ keys, uint32_t n,
+                                                                      const uint64_t* __restrict__ eytz,
+                                                                      const uint64_t* __restrict__ kn,
+                                                                      const float4* __restrict__ segp, int B,
+                                                                      uint32_t* totals, uint16_t* __restrict__ bids) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
-  uint64_t* s_kn = s_e + B;
-  float* s_y = reinterpret_cast<float*>(s_kn + (B + 1));
-  uint32_t* s_hist = reinterpret_cast<uint32_t*>(s_y + (B + 1));
-  load_model(s_kn, s_y, kn, y, B);
-  build_eytzinger(s_e, kn, B);
-  for (int b = threadIdx.x; b < B; b += LC_THREADS) s_hist[b] = 0;
+  uint32_t* s_hist = reinterpret_cast<uint32_t*>(s_e + B);
+  for (int i = threadIdx.x; i < B; i += LC_THREADS) {
+    s_e[i] = (i > 0) ? eytz[i] : 0ull;
+    s_hist[i] = 0;
+  }
   __syncthreads();
-  const size_t base = (size_t)blockIdx.x * LC_TILE;
-#pragma unroll 4
-  for (int j = 0; j < LC_KPT; ++j) {
-    const size_t i = base + (size_t)j * LC_THREADS + threadIdx.x;
-    if (i < n) {
-      const int b = model_bucket(__ldcs(keys + i), s_e, s_kn, s_y, B);
-      atomicAdd(&s_hist[b], 1u);
-      if (bids) bids[i] = (uint16_t)b;
+  const int levels = 31 - __clz(B);
+  const uint32_t step = gridDim.x * LC_THREADS * LC_ILP;
+  for (uint32_t base = blockIdx.x * LC_THREADS * LC_ILP + threadIdx.x; base < n; base += step) {
+    uint64_t k[LC_ILP];
+    int node[LC_ILP];
+#pragma unroll
+    for (int j = 0; j < LC_ILP; ++j) {
+      const uint32_t i = base + j * LC_THREADS;
+      k[j] = (i < n) ? __ldcs(keys + i) : 0ull;
+      node[j] = 1;
+    }
+    for (int l = 0; l < levels; ++l) {
+#pragma unroll
+      for (int j = 0; j < LC_ILP; ++j) node[j] = 2 * node[j] + (s_e[node[j]] <= k[j] ? 1 : 0);
+    }
+#pragma unroll
+    for (int j = 0; j < LC_ILP; ++j) {
+      const uint32_t i = base + j * LC_THREADS;
+      if (i < n) {
+        const int b = model_bucket(k[j], node[j] - B, kn, segp, B);
+        atomicAdd(&s_hist[b], 1u);
+        if (bids) bids[i] = (uint16_t)b;
+      }
     }
   }
   __syncthreads();
@@ -421,123 +446,143 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
   }
 }
 
-// 4. in-bucket sort.
+// 4. in-bucket sort.  One CTA per bucket (two CTAs per SM); the bucket's
+// keys arrive grouped and in input order.  Only positions move: idx holds
+// each key's offset inside the bucket while the keys stay put in shared
+// memory, and the values are gathered by the final order at the end.
+constexpr int BS_WARPS = BS_THREADS / 32;
+constexpr int BS_SORT_BITS = 24;  // bits sorted by counting passes below the highest varying bit
+constexpr int BS_RUN_LIMIT = 64;  // longest run of equal sorted bits finished by insertion
+
 struct BucketSmem {
   uint64_t keys[BS_CAP];
   uint16_t idx[2][BS_CAP];
-  uint32_t hist[BS_THREADS / 32][256];
+  uint32_t cnt[BS_WARPS][128];  // per-warp digit counters / offsets, two 16-bit halves per word
   uint32_t warp_sums[8];
-  uint64_t red[64];
+  uint64_t red[2 * BS_WARPS];
   uint32_t skip, big;
 };
 
-// One stable 8-bit counting pass of the index array idx[cur] by the digit
-// (key >> shift) & 255, into idx[cur ^ 1] (cur flips), unless every key has
-// the same digit.  Warp w owns positions [w * 32 * ipt, (w + 1) * 32 * ipt).
-// Called by every thread of the block.
+__device__ __forceinline__ uint32_t half16(uint32_t word, uint32_t d) { return (word >> ((d & 1u) * 16u)) & 0xffffu; }
+
+// One stable 8-bit counting pass of idx[cur] by the digit (key >> shift) &
+// 255 into idx[cur ^ 1] (cur flips).  Warp w owns positions [w * 32 * ipt,
+// (w + 1) * 32 * ipt) in (j, lane) order.  One sweep gives counts and ranks:
+// the leader of each peer group (8 ballots) adds the group's size to the
+// warp's 16-bit digit counter and gets the group's base back.  The block
+// then turns the counters into offsets (digit-major, warp-minor; 16-bit
+// halves never carry: every count and offset is below BS_CAP) and a second
+// sweep scatters the indices.  A digit shared by every key makes the pass the
+// identity: skipped.  Called by every thread of the block.
 __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt, int shift, int& cur) {
-  constexpr int WARPS = BS_THREADS / 32;
-  constexpr int IPT = BS_CAP / BS_THREADS;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t wrun = (uint32_t)warp * 32u * (uint32_t)ipt;
-  for (int i = tid; i < WARPS * 256; i += BS_THREADS) (&s.hist[0][0])[i] = 0;
-  if (tid == 0) s.skip = 0;
-  __syncthreads();
-  // A. per-warp digit counts over this warp's run of positions.
-  uint32_t d[IPT];
+  uint32_t* row = s.cnt[warp];
+  for (int i = lane; i < 128; i += 32) row[i] = 0;
+  __syncwarp();
+  uint32_t rk[BS_IPT];  // rank within the warp's digit run | digit << 16; ~0: no key
+  uint32_t ix[BS_IPT];  // the index that moves
 #pragma unroll
-  for (int j = 0; j < IPT; ++j) {
-    d[j] = 256u;
-    if (j < ipt) {
+  for (int j = 0; j < BS_IPT; ++j) {
+    rk[j] = 0xffffffffu;
+    ix[j] = 0;
+    if (j < ipt && wrun + j * 32 < cnt) {  // warp-uniform
       const uint32_t pos = wrun + j * 32 + lane;
-      if (pos < cnt) d[j] = (uint32_t)(s.keys[s.idx[cur][pos]] >> shift) & 255u;
-      if (d[j] < 256u) atomicAdd(&s.hist[warp][d[j]], 1u);
+      const bool valid = pos < cnt;
+      const uint32_t x = valid ? s.idx[cur][pos] : 0u;
+      const uint32_t d = valid ? (uint32_t)(s.keys[x] >> shift) & 255u : 0u;
+      uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+      for (int bit = 0; bit < 8; ++bit) {
+        const uint32_t v = (d >> bit) & 1u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, v);
+        peers &= v ? bal : ~bal;
+      }
+      const int leader = valid ? 31 - __clz(peers) : lane;
+      uint32_t b0 = 0;
+      if (valid && lane == leader) b0 = atomicAdd(&row[d >> 1], (uint32_t)__popc(peers) << ((d & 1u) * 16u));
+      b0 = half16(__shfl_sync(0xffffffffu, b0, leader), d);
+      if (valid) {
+        rk[j] = (b0 + __popc(peers & lt_mask)) | (d << 16);
+        ix[j] = x;
+      }
     }
   }
+  if (tid == 0) s.skip = 0;
   __syncthreads();
-  // B. warp offsets per digit and digit bases: thread (digit dg, group g)
-  // scans warps 8g..8g+7 of its digit; the four group sums are combined per
-  // digit (scratch: the index array phase C writes, unused until then).
-  uint32_t* gs = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]);
-  const int dg = tid & 255, grp = tid >> 8;
+  // Offsets.  Thread t owns the digit pair q = t & 127 (one counter word) for
+  // the four warps of quarter t >> 7; quarter sums meet in scratch space of
+  // the destination index array, which the scatter overwrites afterwards.
+  static_assert(BS_THREADS == 512 && BS_WARPS == 16, "four quarters of four warps");
+  const int q = tid & 127, quarter = tid >> 7;
+  uint32_t mine[4];
   uint32_t part = 0;
 #pragma unroll
-  for (int w = 8 * grp; w < 8 * grp + 8; ++w) {
-    const uint32_t c = s.hist[w][dg];
-    s.hist[w][dg] = part;
-    part += c;
+  for (int w = 0; w < 4; ++w) {
+    mine[w] = part;
+    part += s.cnt[quarter * 4 + w][q];
   }
-  gs[grp * 256 + dg] = part;
+  uint32_t* scratch = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]);
+  scratch[quarter * 128 + q] = part;
   __syncthreads();
-  uint32_t count = 0;
-  if (tid < 256) {
-    count = gs[tid] + gs[256 + tid] + gs[512 + tid] + gs[768 + tid];
-    if (count == cnt) s.skip = 1;  // every key has this digit: the pass is the identity
-  }
-  uint32_t incl = 0;
-  if (tid < 256) {
-    incl = warp_inclusive_sum(count);
+  uint32_t t0 = 0, t1 = 0, t2 = 0, pair = 0, incl = 0, lo = 0;
+  if (tid < 128) {
+    t0 = scratch[q];
+    t1 = scratch[128 + q];
+    t2 = scratch[256 + q];
+    const uint32_t tot = t0 + t1 + t2 + scratch[384 + q];
+    lo = tot & 0xffffu;
+    const uint32_t hi = tot >> 16;
+    if (lo == cnt || hi == cnt) s.skip = 1;
+    pair = lo + hi;
+    incl = warp_inclusive_sum(pair);
     if (lane == 31) s.warp_sums[warp] = incl;
   }
   __syncthreads();
-  if (tid < 256) {
+  if (tid < 128) {
     uint32_t pre = 0;
-    for (int w = 0; w < 8; ++w) pre += (w < warp) ? s.warp_sums[w] : 0u;
-    uint32_t run = pre + incl - count;  // digit base
-    for (int g = 0; g < 4; ++g) {
-      const uint32_t t = gs[g * 256 + tid];
-      gs[g * 256 + tid] = run;
-      run += t;
-    }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) pre += (w < warp) ? s.warp_sums[w] : 0u;
+    const uint32_t e = pre + incl - pair;  // base of digit 2q
+    const uint32_t base = e | ((e + lo) << 16);
+    scratch[q] = base;
+    scratch[128 + q] = base + t0;
+    scratch[256 + q] = base + t0 + t1;
+    scratch[384 + q] = base + t0 + t1 + t2;
   }
   __syncthreads();
+  if (s.skip) return;  // block-uniform: every key has the same digit
   {
-    const uint32_t goff = gs[grp * 256 + dg];
+    const uint32_t qoff = scratch[quarter * 128 + q];
 #pragma unroll
-    for (int w = 8 * grp; w < 8 * grp + 8; ++w) s.hist[w][dg] += goff;
+    for (int w = 0; w < 4; ++w) s.cnt[quarter * 4 + w][q] = qoff + mine[w];
   }
   __syncthreads();
-  if (s.skip) return;  // block-uniform
-  // C. stable ranks (peer masks over valid lanes) and the scatter of indices.
 #pragma unroll
-  for (int j = 0; j < IPT; ++j) {
-    if (j >= ipt || wrun + j * 32 >= cnt) break;  // warp-uniform
-    const uint32_t pos = wrun + j * 32 + lane;
-    const bool valid = d[j] < 256u;
-    uint32_t peers = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-    for (int bit = 0; bit < 8; ++bit) {
-      const uint32_t x = (d[j] >> bit) & 1u;
-      const uint32_t bal = __ballot_sync(0xffffffffu, x);
-      peers &= x ? bal : ~bal;
+  for (int j = 0; j < BS_IPT; ++j) {
+    if (rk[j] != 0xffffffffu) {
+      const uint32_t d = rk[j] >> 16;
+      s.idx[cur ^ 1][half16(row[d >> 1], d) + (rk[j] & 0xffffu)] = (uint16_t)ix[j];
     }
-    const int leader = valid ? 31 - __clz(peers) : 0;
-    uint32_t b0 = 0;
-    if (valid && lane == leader) b0 = atomicAdd(&s.hist[warp][d[j]], (uint32_t)__popc(peers));
-    b0 = __shfl_sync(0xffffffffu, b0, leader);
-    if (valid) s.idx[cur ^ 1][b0 + __popc(peers & lt_mask)] = s.idx[cur][pos];
   }
   __syncthreads();
   cur ^= 1;
 }
 
-// One CTA per bucket (its keys arrive grouped and in input order).  Stable
-// sort in shared memory by the 16 highest bits that vary inside the bucket
-// (two 8-bit passes), then every group of keys equal in those bits (short:
-// the model spreads a bucket's keys) finished by a stable insertion sort on
-// the full key.  A bucket with a longer group (measured on the 64M config-5
-// keys: 7.5% of buckets; a 12-bit unstable binning pass instead left a
-// quarter of the buckets with a crowded bin) is re-sorted by full passes over
-// all its varying bits.
-__global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
+// One CTA per bucket.  Stable counting passes over the 24 bits below the
+// highest bit that varies inside the bucket (all varying bits when there are
+// at most 24), then every run of keys equal in those bits (short: measured on
+// the learned workload's keys, the longest runs hold a few dozen keys) is
+// finished by a stable insertion sort on the full key.  A longer run sends
+// the bucket through full passes over all its varying bits instead.
+__global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
     const uint64_t* __restrict__ ukeys, const uint32_t* __restrict__ uvals, const uint32_t* base,
     const uint32_t* totals, uint64_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals, uint64_t* bmin,
     uint64_t* bmax, uint32_t* flags) {
   if (*flags & (LFLAG_OVERFLOW | LFLAG_BAD_MODEL)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BucketSmem& s = *reinterpret_cast<BucketSmem*>(smem_raw);
-  constexpr int WARPS = BS_THREADS / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.x;
   const uint32_t cnt = totals[b];
@@ -555,7 +600,7 @@ __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
   }
   uint64_t mn = ~0ull, mx = 0;
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-    const uint64_t k = ukeys[off + i];
+    const uint64_t k = __ldcs(ukeys + off + i);
     s.keys[i] = k;
     s.idx[0][i] = (uint16_t)i;
     mn = min(mn, k);
@@ -568,48 +613,52 @@ __global__ void __launch_bounds__(BS_THREADS) bucket_sort_kernel(
   }
   if (lane == 0) {
     s.red[warp] = mn;
-    s.red[32 + warp] = mx;
+    s.red[BS_WARPS + warp] = mx;
   }
   if (tid == 0) s.big = 0;
   __syncthreads();
   mn = s.red[0];
-  mx = s.red[32];
-  for (int w = 1; w < WARPS; ++w) {
+  mx = s.red[BS_WARPS];
+#pragma unroll
+  for (int w = 1; w < BS_WARPS; ++w) {
     mn = min(mn, s.red[w]);
-    mx = max(mx, s.red[32 + w]);
+    mx = max(mx, s.red[BS_WARPS + w]);
   }
   const int vbits = (mn == mx) ? 0 : 64 - __clzll((long long)(mn ^ mx));
   const int ipt = (int)((cnt + BS_THREADS - 1) / BS_THREADS);
   int cur = 0;
-  if (vbits <= 16) {
+  if (vbits <= BS_SORT_BITS) {
     for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
   } else {
-    const int lo = vbits - 16;
+    const int lo = vbits - BS_SORT_BITS;
     bucket_pass(s, cnt, ipt, lo, cur);
     bucket_pass(s, cnt, ipt, lo + 8, cur);
+    bucket_pass(s, cnt, ipt, lo + 16, cur);
+    uint16_t* ix = s.idx[cur];
     for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-      const uint64_t h = s.keys[s.idx[cur][i]] >> lo;
-      if (i > 0 && (s.keys[s.idx[cur][i - 1]] >> lo) == h) continue;  // not a group start
+      const uint64_t h = s.keys[ix[i]] >> lo;
+      if (i > 0 && (s.keys[ix[i - 1]] >> lo) == h) continue;  // not a run start
       uint32_t e = i + 1;
-      while (e < cnt && e - i <= (uint32_t)BS_GROUP && (s.keys[s.idx[cur][e]] >> lo) == h) ++e;
-      if (e - i > (uint32_t)BS_GROUP) {
+      while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && (s.keys[ix[e]] >> lo) == h) ++e;
+      if (e - i > (uint32_t)BS_RUN_LIMIT) {
         s.big = 1;
         continue;
       }
-      for (uint32_t a = i + 1; a < e; ++a) {  // stable: strict comparison
-        const uint16_t x = s.idx[cur][a];
+      for (uint32_t a = i + 1; a < e; ++a) {  // stable: only strictly greater keys move up
+        const uint16_t x = ix[a];
         const uint64_t kx = s.keys[x];
         uint32_t c = a;
-        while (c > i && s.keys[s.idx[cur][c - 1]] > kx) {
-          s.idx[cur][c] = s.idx[cur][c - 1];
+        while (c > i && s.keys[ix[c - 1]] > kx) {
+          ix[c] = ix[c - 1];
           --c;
         }
-        s.idx[cur][c] = x;
+        ix[c] = x;
       }
     }
     __syncthreads();
-    if (s.big) {  // block-uniform: start over with full passes
-      for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[cur][i] = (uint16_t)i;
+    if (s.big) {  // block-uniform: start over with full passes over every varying bit
+      for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[0][i] = (uint16_t)i;
+      cur = 0;
       __syncthreads();
       for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
     }
@@ -706,6 +755,8 @@ struct gtc_learned_model {
   int B = 0;
   uint64_t* knots = nullptr;   // [B + 1]
   float* heights = nullptr;    // [B + 1]
+  uint64_t* eytz = nullptr;    // [B]: interior knots in Eytzinger order (derived before each sort)
+  float4* segp = nullptr;      // [B]: per-segment bucket lines (derived before each sort)
   float* m1 = nullptr;         // Adam moments [B + 1]
   float* m2 = nullptr;
   float* grad = nullptr;       // [B + 1]
@@ -725,8 +776,28 @@ gtc_status cuda_fail(gtc_ctx* ctx, const char* what, cudaError_t e) {
     if (_e != cudaSuccess) return cuda_fail(ctx, #expr, _e); \
   } while (0)
 
-// Eytzinger knots + sorted knots + heights + per-bucket counters.
-size_t model_smem_bytes(int B) { return (size_t)B * 8 + (size_t)(B + 1) * 12 + (size_t)B * 4; }
+// Count kernel: Eytzinger knots + per-bucket counters.
+size_t count_smem_bytes(int B) { return (size_t)B * 8 + (size_t)B * 4; }
+
+// Derives the sort-time model arrays from the knots and heights.
+gtc_status prepare_model(gtc_ctx* ctx, const gtc_learned_model* m, uint32_t* d_flags, cudaStream_t s) {
+  learned_prepare_kernel<<<ceil_div(m->B, 256), 256, 0, s>>>(m->knots, m->heights, m->B, m->eytz, m->segp, d_flags);
+  LTRY(ctx, cudaGetLastError());
+  return GTC_OK;
+}
+
+// The count kernel over the keys: one resident CTA per SM.
+gtc_status launch_count(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys, uint32_t n, uint32_t* totals,
+                        uint16_t* bids, cudaStream_t s) {
+  const int B = m->B;
+  LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, count_smem_bytes(MAX_BUCKETS)));
+  const Launch L = context_launch(ctx, reinterpret_cast<gtc_stream_t>(s));
+  const uint32_t grid = max(1u, min((uint32_t)L.num_sms, ceil_div(n, LC_THREADS * LC_ILP)));
+  learned_count_kernel<<<grid, LC_THREADS, count_smem_bytes(B), s>>>(keys, n, m->eytz, m->knots, m->segp, B, totals,
+                                                                     bids);
+  LTRY(ctx, cudaGetLastError());
+  return GTC_OK;
+}
 
 gtc_status prepare_sample(gtc_ctx* ctx, gtc_learned_model* m, const uint64_t* sorted, uint32_t n, uint32_t stride,
                           cudaStream_t s) {
@@ -752,7 +823,7 @@ GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learn
   if (!ctx || !out) return GTC_ERR_INVALID_ARG;
   *out = nullptr;
   if (buckets < 2 || buckets > MAX_BUCKETS || (buckets & (buckets - 1)))
-    return context_error(ctx, GTC_ERR_INVALID_ARG, "buckets must be a power of two in [2, 8192]", cudaSuccess);
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "buckets must be a power of two in [2, 16384]", cudaSuccess);
   gtc_learned_model* m = new (std::nothrow) gtc_learned_model();
   if (!m) return GTC_ERR_OOM;
   m->B = buckets;
@@ -763,6 +834,8 @@ GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learn
   if (e == cudaSuccess) e = cudaMalloc(&m->m2, nb * 4);
   if (e == cudaSuccess) e = cudaMalloc(&m->grad, nb * 4);
   if (e == cudaSuccess) e = cudaMalloc(&m->loss, 256);
+  if (e == cudaSuccess) e = cudaMalloc(&m->eytz, (size_t)buckets * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&m->segp, (size_t)buckets * 16);
   if (e != cudaSuccess) {
     gtc_learned_model_destroy(m);
     return cuda_fail(ctx, "allocating the learned model", e);
@@ -773,7 +846,7 @@ GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learn
 
 GTC_API gtc_status gtc_learned_model_destroy(gtc_learned_model* m) {
   if (!m) return GTC_OK;
-  void* ptrs[] = {m->knots, m->heights, m->m1, m->m2, m->grad, m->loss, m->sample};
+  void* ptrs[] = {m->knots, m->heights, m->m1, m->m2, m->grad, m->loss, m->sample, m->eytz, m->segp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete m;
@@ -809,8 +882,10 @@ GTC_API gtc_status gtc_learned_train_u64(gtc_ctx* ctx, gtc_learned_model* m, con
   knots_init_kernel<<<ceil_div(B + 1, 256), 256, 0, s>>>(m->sample, m->ns, B, m->knots, m->heights, m->m1, m->m2);
   LTRY(ctx, cudaGetLastError());
   for (int it = 1; it <= iters; ++it) {
+    // learning rate: lr at the first step, decaying exponentially to lr / 10^4 at the last
+    const float lr_t = (iters > 1) ? lr * powf(1e-4f, (float)(it - 1) / (float)(iters - 1)) : lr;
     grad_kernel<<<ceil_div(B + 1, 128), 128, 0, s>>>(m->sample, m->ns, m->knots, m->heights, B, m->grad);
-    adam_kernel<<<1, 1024, 0, s>>>(m->heights, m->grad, m->m1, m->m2, B, lr, it);
+    adam_kernel<<<1, 1024, 0, s>>>(m->heights, m->grad, m->m1, m->m2, B, lr_t, it);
   }
   LTRY(ctx, cudaGetLastError());
   LTRY(ctx, cudaMemsetAsync(m->loss, 0, 4, s));
@@ -846,11 +921,9 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
   const int B = m->B;
   LTRY(ctx, cudaMemsetAsync(d_counts, 0, (size_t)B * 4, s));
   if (n == 0) return GTC_OK;
-  LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, model_smem_bytes(MAX_BUCKETS)));
-  learned_count_kernel<<<ceil_div(n, LC_TILE), LC_THREADS, model_smem_bytes(B), s>>>(keys, n, m->knots, m->heights, B,
-                                                                                     d_counts, nullptr);
-  LTRY(ctx, cudaGetLastError());
-  return GTC_OK;
+  gtc_status st = prepare_model(ctx, m, nullptr, s);
+  if (st != GTC_OK) return st;
+  return launch_count(ctx, m, keys, n, d_counts, nullptr, s);
 }
 
 GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys,
@@ -872,12 +945,9 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
                          cudaSuccess);
   LearnedWorkspace W;
   learned_ws_layout(n, B, &W, reinterpret_cast<char*>(ws));
-  const uint32_t tiles = ceil_div(n, LC_TILE);
   const uint32_t ptiles = ceil_div(n, LP_TILE);
-  const size_t msmem = model_smem_bytes(B);
   const int lb = 31 - __builtin_clz((unsigned)B);  // bucket-id bits
   const int db1 = (lb + 1) / 2, db2 = lb - db1;      // digit widths of the two passes (<= 7 each)
-  LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, model_smem_bytes(MAX_BUCKETS)));
   LTRY(ctx, kernel_setup(learned_pass_kernel<true>, LP_THREADS, sizeof(LpSmem)));
   LTRY(ctx, kernel_setup(learned_pass_kernel<false>, LP_THREADS, sizeof(LpSmem)));
   LTRY(ctx, kernel_setup(bucket_sort_kernel, BS_THREADS, sizeof(BucketSmem)));
@@ -885,7 +955,9 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
   LTRY(ctx, cudaMemsetAsync(W.misc, 0, 256, s));
   LTRY(ctx, cudaMemsetAsync(W.totals, 0, (size_t)B * 4, s));
   LTRY(ctx, cudaMemsetAsync(W.desc, 0, 2 * W.desc_words * 4, s));
-  learned_count_kernel<<<tiles, LC_THREADS, msmem, s>>>(keys, n, m->knots, m->heights, B, W.totals, W.bid);
+  gtc_status st = prepare_model(ctx, m, d_flags, s);
+  if (st == GTC_OK) st = launch_count(ctx, m, keys, n, W.totals, W.bid, s);
+  if (st != GTC_OK) return st;
   learned_scan_kernel<<<1, 1024, 0, s>>>(W.totals, B, db1, m->heights, W.base, W.off1, W.off2, d_flags);
   learned_pass_kernel<true><<<ptiles, LP_THREADS, sizeof(LpSmem), s>>>(
       keys, vals, W.bid, db2 ? W.tkeys : W.ukeys, db2 ? W.tvals : W.uvals, W.bid2, n, 0, (1u << db1) - 1, W.off1,

@@ -562,7 +562,10 @@ class LearnedModel:
                                                            hy.ctypes.data_as(ctypes.c_void_p)))
         return kn, hy
 
-    def train(self, sorted_keys, stride: int = 100, iters: int = 100, lr: float = 1e-4) -> float:
+    def train(self, sorted_keys, stride: int = 100, iters: int = 600, lr: float = 0.05) -> float:
+        """Knots at the quantiles of every stride-th key of sorted_keys, heights
+        from the key-space uniform CDF, then `iters` Adam steps on the heights
+        (learning rate decaying from lr to lr / 10^4).  Returns the final loss."""
         torch = _torch()
         loss = torch.zeros(1, dtype=torch.float32, device=sorted_keys.device)
         self.ctx.check(self.ctx.L.gtc_learned_train_u64(self.ctx.h, self.h, _ptr(sorted_keys), sorted_keys.numel(),
@@ -600,10 +603,10 @@ class LearnedModel:
 
 def learned_buckets_for(n: int) -> int:
     """Bucket count for n keys: 2^12, raised to the next power of two while the
-    average bucket would exceed 8192 keys (the on-chip bucket sort holds at
-    most 16384), capped at 8192."""
+    average bucket would exceed 4096 keys (the on-chip bucket sort holds at
+    most 8192), capped at 16384."""
     b = 4096
-    while n / b > 8192 and b < 8192:
+    while n / b > 4096 and b < 16384:
         b *= 2
     return b
 

@@ -615,14 +615,21 @@ double orc_pwl_loss_grad(const uint64_t* s, uint32_t ns, const uint64_t* kn, con
 }
 
 void orc_pwl_buckets(const uint64_t* keys, uint32_t n, const uint64_t* kn, const float* y, int B, uint32_t* out) {
+  // The bucket line of the GPU model, operation for operation in FP32 with
+  // round-to-nearest and no contraction: t = B*y0 + c * float(key - k0),
+  // c = B*(y1 - y0) / float(k1 - k0), clamped to B*y1, truncated.
+  const float fb = (float)B;
   for (uint32_t i = 0; i < n; ++i) {
     const int seg = pwl_segment(keys[i], kn, B);
     const uint64_t k0 = kn[seg], k1 = kn[seg + 1];
-    const double w = (k1 > k0) ? (double)(keys[i] - k0) / (double)(k1 - k0) : 0.0;
-    double F = (double)y[seg] + ((double)y[seg + 1] - (double)y[seg]) * w;
-    F = std::min(std::max(F, (double)y[seg]), (double)y[seg + 1]);
-    long b = (long)(F * B);
-    out[i] = (uint32_t)std::min<long>(std::max<long>(b, 0), B - 1);
+    const float y0 = y[seg], y1 = y[seg + 1];
+    const float dy = fb * (y1 - y0);
+    const float c = (k1 > k0 && dy > 0.0f) ? dy / (float)(k1 - k0) : 0.0f;
+    const float a = fb * y0, amax = fb * y1;
+    float t = a + c * (float)(keys[i] - k0);
+    t = std::min(t, amax);
+    const int b = (int)t;
+    out[i] = (uint32_t)std::min(std::max(b, 0), B - 1);
   }
 }
 

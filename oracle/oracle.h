@@ -162,8 +162,10 @@ int orc_max_threads(void);
  * Double precision; the checker of the GPU backward kernel. */
 double orc_pwl_loss_grad(const uint64_t* sample, uint32_t ns, const uint64_t* kn, const float* y, int B,
                          double* grad);
-/* Bucket of each key under the model: floor(B * F), F clamped to the
- * segment's end heights, in double precision. */
+/* Bucket of each key under the model, the GPU's FP32 bucket line operation
+ * for operation: in the key's segment s (last knot <= key),
+ * t = B*y[s] + c * float(key - kn[s]) with c = B*(y[s+1] - y[s]) /
+ * float(kn[s+1] - kn[s]), clamped to B*y[s+1], truncated. */
 void orc_pwl_buckets(const uint64_t* keys, uint32_t n, const uint64_t* kn, const float* y, int B, uint32_t* out);
 
 #ifdef __cplusplus
