@@ -331,6 +331,8 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     src_v = torch.arange(n, dtype=torch.int32, device="cuda")
     if variant is not None:
         ctx.set_sort_variant(kb, variant)
+    else:  # the autotuner's pick for these keys (cached per key width, bits and ceil(log2 n))
+        ctx.autotune_sort(kb, n, 0, kb, keys=src_k, reps=3)
     ws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
     k, v = torch.empty_like(src_k), torch.empty_like(src_v)
     ka, va = torch.empty_like(src_k), torch.empty_like(src_v)
@@ -367,7 +369,8 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
             "pass_ms": round(avg, 5), "pass_hbm_frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
             "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4),
             "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
-            "sort_variant": ctx.get_sort_variant(kb), "sorted_ok": ok}, stages
+            "sort_variant": variant if variant is not None else gtc.autotune_lookup(kb, kb, n),
+            "sorted_ok": ok}, stages
 
 
 def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
@@ -403,6 +406,8 @@ def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
     wk, wv = torch.empty_like(keys), torch.empty_like(vals)
     ka, va = torch.empty_like(keys), torch.empty_like(vals)
     sws = ctx.workspace(gtc.OP_SORT_PAIRS, n, 64)
+    # the plain sort runs the autotuner's pick for these keys
+    ctx.autotune_sort(64, n, 0, 64, keys=keys, reps=2)
     flags = []
 
     def learned_step():
@@ -436,7 +441,8 @@ def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
     out = {"learned_mkeys_s": round(n / (learned_ms * 1e-3) / 1e6, 1), "learned_ms": round(learned_ms, 4),
            "plain_mkeys_s": round(n / (plain_ms * 1e-3) / 1e6, 1), "plain_ms": round(plain_ms, 4),
            "speedup_vs_plain": round(plain_ms / learned_ms, 3), "identical": identical, "flags": fl, "n": n,
-           "buckets": B, "train_loss": loss, "train_s": round(train_s, 3),
+           "buckets": B, "plain_sort_variant": gtc.autotune_lookup(64, 64, n), "train_loss": loss,
+           "train_s": round(train_s, 3),
            "bucket_max_over_mean": round(float(counts.max()) / (n / B), 3),
            "shifted_n": int(shifted.numel()), "shifted_flags": int(sflags.item()), "shifted_exact": shifted_ok}
     model.close()

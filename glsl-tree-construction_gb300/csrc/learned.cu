@@ -244,10 +244,16 @@ __global__ void __launch_bounds__(LC_THREADS, 1) learned_count_kernel(const uint
                                                                       const float4* __restrict__ segp, int B,
                                                                       uint32_t* totals, uint16_t* __restrict__ bids) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* s_e = reinterpret_cast<uint64_t*>(smem_raw);
-  uint32_t* s_hist = reinterpret_cast<uint32_t*>(s_e + B);
+  // The tree's knots as two word arrays: a level compares the high words and
+  // reads the low word only where they are equal, so most levels move 4
+  // bytes per lane instead of 8 (half the shared-memory wavefronts).
+  uint32_t* s_hi = reinterpret_cast<uint32_t*>(smem_raw);
+  uint32_t* s_lo = s_hi + B;
+  uint32_t* s_hist = s_lo + B;
   for (int i = threadIdx.x; i < B; i += LC_THREADS) {
-    s_e[i] = (i > 0) ? eytz[i] : 0ull;
+    const uint64_t e = (i > 0) ? eytz[i] : 0ull;
+    s_hi[i] = (uint32_t)(e >> 32);
+    s_lo[i] = (uint32_t)e;
     s_hist[i] = 0;
   }
   __syncthreads();
@@ -262,9 +268,20 @@ __global__ void __launch_bounds__(LC_THREADS, 1) learned_count_kernel(const uint
       k[j] = (i < n) ? __ldcs(keys + i) : 0ull;
       node[j] = 1;
     }
+    uint32_t kh[LC_ILP], kl[LC_ILP];
+#pragma unroll
+    for (int j = 0; j < LC_ILP; ++j) {
+      kh[j] = (uint32_t)(k[j] >> 32);
+      kl[j] = (uint32_t)k[j];
+    }
     for (int l = 0; l < levels; ++l) {
 #pragma unroll
-      for (int j = 0; j < LC_ILP; ++j) node[j] = 2 * node[j] + (s_e[node[j]] <= k[j] ? 1 : 0);
+      for (int j = 0; j < LC_ILP; ++j) {
+        const uint32_t h = s_hi[node[j]];
+        // knot <= key: high words decide unless equal
+        const bool right = (h != kh[j]) ? (h < kh[j]) : (s_lo[node[j]] <= kl[j]);
+        node[j] = 2 * node[j] + (right ? 1 : 0);
+      }
     }
 #pragma unroll
     for (int j = 0; j < LC_ILP; ++j) {
@@ -448,65 +465,77 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
 
 // 4. in-bucket sort.  One CTA per bucket (two CTAs per SM); the bucket's
 // keys arrive grouped and in input order.  Only positions move: idx holds
-// each key's offset inside the bucket while the keys stay put in shared
-// memory, and the values are gathered by the final order at the end.
+// each key's offset inside the bucket, and the counting passes read a 32-bit
+// sort word per key in shared memory (the 24 highest bits that vary inside
+// the bucket), so a pass extracts its digit with one byte select.  The full
+// keys stay in global memory (read twice at the start, then cached); the
+// output gathers keys and values by the final order.
 constexpr int BS_WARPS = BS_THREADS / 32;
 constexpr int BS_SORT_BITS = 24;  // bits sorted by counting passes below the highest varying bit
 constexpr int BS_RUN_LIMIT = 64;  // longest run of equal sorted bits finished by insertion
 
 struct BucketSmem {
-  uint64_t keys[BS_CAP];
-  uint16_t idx[2][BS_CAP];
+  uint32_t sk[BS_CAP];          // sort words: key bits [lo, lo + 24)
+  uint16_t idx[2][BS_CAP];      // positions; the destination array doubles as the ranking's peer masks
   uint32_t cnt[BS_WARPS][128];  // per-warp digit counters / offsets, two 16-bit halves per word
   uint32_t warp_sums[8];
   uint64_t red[2 * BS_WARPS];
   uint32_t skip, big;
 };
+static_assert(sizeof(uint16_t) * BS_CAP >= sizeof(uint32_t) * 256 * BS_WARPS, "peer masks fit in an index array");
 
 __device__ __forceinline__ uint32_t half16(uint32_t word, uint32_t d) { return (word >> ((d & 1u) * 16u)) & 0xffffu; }
 
-// One stable 8-bit counting pass of idx[cur] by the digit (key >> shift) &
-// 255 into idx[cur ^ 1] (cur flips).  Warp w owns positions [w * 32 * ipt,
-// (w + 1) * 32 * ipt) in (j, lane) order.  One sweep gives counts and ranks:
-// the leader of each peer group (8 ballots) adds the group's size to the
-// warp's 16-bit digit counter and gets the group's base back.  The block
-// then turns the counters into offsets (digit-major, warp-minor; 16-bit
+// One stable 8-bit counting pass of idx[cur] into idx[cur ^ 1] (cur flips).
+// The digit of the key at offset x is byte `shift / 8` of sk[x], or, with
+// gkeys, (gkeys[x] >> shift) & 255 (the rare full passes beyond the sort
+// word).  Warp w owns positions [w * 32 * ipt, (w + 1) * 32 * ipt) in
+// (j, lane) order.  One sweep gives counts and ranks: every lane sets its bit
+// in the warp's peer-mask word of its digit (shared atomicOr, the words kept
+// in the destination index array, which is free until the scatter), and the
+// highest lane of each peer group adds the group's size to the warp's 16-bit
+// digit counter, gets the group's base back and clears the mask word.  The
+// block then turns the counters into offsets (digit-major, warp-minor; 16-bit
 // halves never carry: every count and offset is below BS_CAP) and a second
 // sweep scatters the indices.  A digit shared by every key makes the pass the
 // identity: skipped.  Called by every thread of the block.
-__device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt, int shift, int& cur) {
+__device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt, int shift, int& cur,
+                                            const uint64_t* gkeys) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t wrun = (uint32_t)warp * 32u * (uint32_t)ipt;
   uint32_t* row = s.cnt[warp];
+  uint32_t* mw = reinterpret_cast<uint32_t*>(s.idx[cur ^ 1]) + warp * 256;
   for (int i = lane; i < 128; i += 32) row[i] = 0;
+  for (int i = lane; i < 256; i += 32) mw[i] = 0;
   __syncwarp();
-  uint32_t rk[BS_IPT];  // rank within the warp's digit run | digit << 16; ~0: no key
-  uint32_t ix[BS_IPT];  // the index that moves
+  const uint32_t sel = 0x4440u + (uint32_t)(shift >> 3);  // byte select of the sort word
+  // Per key: rank within the warp's digit run (< 32 * BS_IPT = 512: 9 bits) |
+  // digit << 9 | moving index << 17 (< BS_CAP: 13 bits); ~0: no key.
+  static_assert(32 * BS_IPT <= 512 && BS_CAP <= 8192, "rank, digit and index pack into 30 bits");
+  uint32_t rk[BS_IPT];
 #pragma unroll
   for (int j = 0; j < BS_IPT; ++j) {
     rk[j] = 0xffffffffu;
-    ix[j] = 0;
     if (j < ipt && wrun + j * 32 < cnt) {  // warp-uniform
       const uint32_t pos = wrun + j * 32 + lane;
       const bool valid = pos < cnt;
       const uint32_t x = valid ? s.idx[cur][pos] : 0u;
-      const uint32_t d = valid ? (uint32_t)(s.keys[x] >> shift) & 255u : 0u;
-      uint32_t peers = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-      for (int bit = 0; bit < 8; ++bit) {
-        const uint32_t v = (d >> bit) & 1u;
-        const uint32_t bal = __ballot_sync(0xffffffffu, v);
-        peers &= v ? bal : ~bal;
-      }
+      uint32_t d = 0;
+      if (valid) d = gkeys ? (uint32_t)(gkeys[x] >> shift) & 255u : __byte_perm(s.sk[x], 0u, sel);
+      if (valid) atomicOr(&mw[d], 1u << lane);
+      __syncwarp();
+      const uint32_t peers = valid ? mw[d] : 0u;
+      __syncwarp();  // every lane has read its mask word before the leaders clear them
       const int leader = valid ? 31 - __clz(peers) : lane;
       uint32_t b0 = 0;
-      if (valid && lane == leader) b0 = atomicAdd(&row[d >> 1], (uint32_t)__popc(peers) << ((d & 1u) * 16u));
-      b0 = half16(__shfl_sync(0xffffffffu, b0, leader), d);
-      if (valid) {
-        rk[j] = (b0 + __popc(peers & lt_mask)) | (d << 16);
-        ix[j] = x;
+      if (valid && lane == leader) {
+        b0 = atomicAdd(&row[d >> 1], (uint32_t)__popc(peers) << ((d & 1u) * 16u));
+        mw[d] = 0;
       }
+      b0 = half16(__shfl_sync(0xffffffffu, b0, leader), d);
+      if (valid) rk[j] = (b0 + __popc(peers & lt_mask)) | (d << 9) | (x << 17);
+      __syncwarp();  // the words are clear before the next key's atomicOr
     }
   }
   if (tid == 0) s.skip = 0;
@@ -562,20 +591,21 @@ __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt
 #pragma unroll
   for (int j = 0; j < BS_IPT; ++j) {
     if (rk[j] != 0xffffffffu) {
-      const uint32_t d = rk[j] >> 16;
-      s.idx[cur ^ 1][half16(row[d >> 1], d) + (rk[j] & 0xffffu)] = (uint16_t)ix[j];
+      const uint32_t d = (rk[j] >> 9) & 255u;
+      s.idx[cur ^ 1][half16(row[d >> 1], d) + (rk[j] & 511u)] = (uint16_t)(rk[j] >> 17);
     }
   }
   __syncthreads();
   cur ^= 1;
 }
 
-// One CTA per bucket.  Stable counting passes over the 24 bits below the
-// highest bit that varies inside the bucket (all varying bits when there are
-// at most 24), then every run of keys equal in those bits (short: measured on
-// the learned workload's keys, the longest runs hold a few dozen keys) is
-// finished by a stable insertion sort on the full key.  A longer run sends
-// the bucket through full passes over all its varying bits instead.
+// One CTA per bucket.  Stable counting passes over the sort word (the 24
+// bits below the highest bit that varies inside the bucket; all varying bits
+// when there are at most 24), then every run of keys equal in those bits
+// (short: measured on the learned workload's keys, the longest runs hold a
+// few dozen keys) is finished by a stable insertion sort on the full key.  A
+// longer run sends the bucket through full passes over all its varying bits
+// instead.
 __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
     const uint64_t* __restrict__ ukeys, const uint32_t* __restrict__ uvals, const uint32_t* base,
     const uint32_t* totals, uint64_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals, uint64_t* bmin,
@@ -598,11 +628,10 @@ __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
     if (tid == 0) atomicOr(flags, LFLAG_OVERFLOW);
     return;
   }
+  const uint64_t* keys = ukeys + off;
   uint64_t mn = ~0ull, mx = 0;
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-    const uint64_t k = __ldcs(ukeys + off + i);
-    s.keys[i] = k;
-    s.idx[0][i] = (uint16_t)i;
+    const uint64_t k = keys[i];
     mn = min(mn, k);
     mx = max(mx, k);
   }
@@ -625,30 +654,32 @@ __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
     mx = max(mx, s.red[BS_WARPS + w]);
   }
   const int vbits = (mn == mx) ? 0 : 64 - __clzll((long long)(mn ^ mx));
+  const int lo = vbits > BS_SORT_BITS ? vbits - BS_SORT_BITS : 0;
+  for (uint32_t i = tid; i < cnt; i += BS_THREADS) {  // second read: cached
+    s.sk[i] = (uint32_t)(keys[i] >> lo) & 0xffffffu;
+    s.idx[0][i] = (uint16_t)i;
+  }
+  __syncthreads();
   const int ipt = (int)((cnt + BS_THREADS - 1) / BS_THREADS);
   int cur = 0;
-  if (vbits <= BS_SORT_BITS) {
-    for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
-  } else {
-    const int lo = vbits - BS_SORT_BITS;
-    bucket_pass(s, cnt, ipt, lo, cur);
-    bucket_pass(s, cnt, ipt, lo + 8, cur);
-    bucket_pass(s, cnt, ipt, lo + 16, cur);
+  const int np = (min(vbits, BS_SORT_BITS) + 7) / 8;
+  for (int p = 0; p < np; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur, nullptr);
+  if (vbits > BS_SORT_BITS) {
     uint16_t* ix = s.idx[cur];
     for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-      const uint64_t h = s.keys[ix[i]] >> lo;
-      if (i > 0 && (s.keys[ix[i - 1]] >> lo) == h) continue;  // not a run start
+      const uint32_t h = s.sk[ix[i]];
+      if (i > 0 && s.sk[ix[i - 1]] == h) continue;  // not a run start
       uint32_t e = i + 1;
-      while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && (s.keys[ix[e]] >> lo) == h) ++e;
+      while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && s.sk[ix[e]] == h) ++e;
       if (e - i > (uint32_t)BS_RUN_LIMIT) {
         s.big = 1;
         continue;
       }
       for (uint32_t a = i + 1; a < e; ++a) {  // stable: only strictly greater keys move up
         const uint16_t x = ix[a];
-        const uint64_t kx = s.keys[x];
+        const uint64_t kx = keys[x];
         uint32_t c = a;
-        while (c > i && s.keys[ix[c - 1]] > kx) {
+        while (c > i && keys[ix[c - 1]] > kx) {
           ix[c] = ix[c - 1];
           --c;
         }
@@ -660,12 +691,12 @@ __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
       for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[0][i] = (uint16_t)i;
       cur = 0;
       __syncthreads();
-      for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur);
+      for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur, keys);
     }
   }
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
     const uint16_t x = s.idx[cur][i];
-    out_keys[off + i] = s.keys[x];
+    out_keys[off + i] = keys[x];
     out_vals[off + i] = uvals[off + x];
   }
   if (tid == 0) {

@@ -17,6 +17,7 @@
 //   6. scatter into shared memory in tile-local digit order, then coalesced
 //      writes of each digit run to its global position.
 
+#include <cstddef>
 #include <cstdio>
 
 #include <atomic>
@@ -487,7 +488,7 @@ struct OnesweepSmem {
   uint32_t tile_id;
 };
 
-template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB, int LBW, bool EARLY, bool L2H = false>
+template <class K, int THREADS, int KPT, bool HAS_VALS, int MINB, int LBW, int RANK, bool L2H = false>
 __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            K* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, uint32_t dmask,
@@ -510,6 +511,15 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   const int warp = tid >> 5;
 
   for (int i = tid; i < WARPS * RADIX; i += THREADS) (&s.warp_hist[0][0])[i] = 0;
+  // RANK 2: three rotating per-warp arrays of digit peer masks live in the
+  // key/value staging space, which is free until the scatter; zeroed here.
+  constexpr int MATCH_WORDS = 3 * WARPS * RADIX;
+  if constexpr (RANK == 2) {
+    static_assert(sizeof(s.keys) + sizeof(s.vals) >= MATCH_WORDS * 4, "peer masks fit in the staging space");
+    static_assert(offsetof(S, vals) == sizeof(s.keys), "keys and values are contiguous");
+    uint4* m4 = reinterpret_cast<uint4*>(s.keys);
+    for (int i = tid; i < MATCH_WORDS / 4; i += THREADS) m4[i] = make_uint4(0, 0, 0, 0);
+  }
   if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
   // Blocks start in about index order, so the ticket is usually close to
   // this block's index: warm L2 with that tile while the ticket is in flight
@@ -555,8 +565,8 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
 
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* my_hist = s.warp_hist[warp];
-  uint32_t rank[KPT];  // !EARLY: rank within the warp's digit run | digit << 16
-  if (EARLY) {
+  uint32_t rank[KPT];  // RANK 1, 2: rank within the warp's digit run | digit << 16
+  if (RANK == 0) {
     // 3. early per-warp digit counts: one shared atomic per key (one per warp
     // when all 32 lanes share the digit, the low-entropy case).
 #pragma unroll
@@ -568,6 +578,33 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
       } else {
         atomicAdd(&my_hist[d], 1u);
       }
+    }
+  } else if (RANK == 2) {
+    // 3''. counts and warp ranks in one sweep, the peer mask from one shared
+    // atomicOr per key instead of 8 ballots: every lane sets its bit in the
+    // warp's mask word of its digit, and after __syncwarp the word holds the
+    // peer group.  Masks rotate over three arrays: the leader clears the
+    // word of key j - 1 after the __syncwarp of key j (every lane has read
+    // it by then), and that array is next written for key j + 2, after the
+    // __syncwarp of key j + 1.
+    uint32_t* mbase = reinterpret_cast<uint32_t*>(s.keys) + warp * RADIX;
+    uint32_t prev_d = 0;
+    bool prev_lead = false;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      uint32_t* mw = mbase + (j % 3) * (WARPS * RADIX);
+      const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
+      atomicOr(&mw[d], 1u << lane);
+      __syncwarp();
+      if (j > 0 && prev_lead) mbase[((j - 1) % 3) * (WARPS * RADIX) + prev_d] = 0;
+      const uint32_t peers = mw[d];
+      const int leader = 31 - __clz(peers);
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      rank[j] = (base + __popc(peers & lt_mask)) | (d << 16);
+      prev_d = d;
+      prev_lead = lane == leader;
     }
   } else {
     // 3'. counts and warp ranks in one sweep: the peer group's leader adds the
@@ -613,7 +650,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
   }
   __syncthreads();
 
-  if (EARLY) {
+  if (RANK == 0) {
     // 5. stable ranks by warp multisplit (8 __ballot_sync give the peer mask;
     // the highest peer advances the warp's digit cursor and broadcasts the old
     // value) and the scatter into tile-local digit order.
@@ -891,12 +928,14 @@ struct Variant {
   int kind;
   int min_blocks;  // kind 0: __launch_bounds__ minimum CTAs per SM (caps registers: an
                    // explicit 1 lets the compiler spend ~116 registers and run slower)
-  int early;       // kind 0: 1 = per-key early counts, then ranks; 0 = counts and ranks in one sweep
+  int rank;        // kind 0: 0 = per-key early counts, then ballot ranks; 1 = counts and ballot ranks in
+                   // one sweep; 2 = counts and ranks in one sweep, peer masks from shared atomicOr
 };
-constexpr Variant kVariants[] = {{256, 16, 0, 3, 1}, {384, 16, 0, 2, 1}, {512, 12, 0, 2, 1}, {256, 16, 1, 1, 1},
-                                 {256, 16, 2, 1, 1}, {512, 8, 2, 1, 1},  {256, 24, 2, 1, 1}, {256, 16, 0, 4, 1},
-                                 {512, 8, 0, 2, 1},  {384, 12, 0, 3, 1}, {256, 16, 0, 3, 0}, {384, 16, 0, 2, 0},
-                                 {512, 12, 0, 2, 0}, {256, 24, 0, 2, 0}, {256, 16, 4, 3, 1}, {512, 12, 4, 2, 0}};
+constexpr Variant kVariants[] = {{256, 16, 0, 3, 0}, {384, 16, 0, 2, 0}, {512, 12, 0, 2, 0}, {256, 16, 1, 1, 0},
+                                 {256, 16, 2, 1, 0}, {512, 8, 2, 1, 0},  {256, 24, 2, 1, 0}, {256, 16, 0, 4, 0},
+                                 {512, 8, 0, 2, 0},  {384, 12, 0, 3, 0}, {256, 16, 0, 3, 1}, {384, 16, 0, 2, 1},
+                                 {512, 12, 0, 2, 1}, {256, 24, 0, 2, 1}, {256, 16, 4, 3, 0}, {512, 12, 4, 2, 1},
+                                 {256, 16, 4, 3, 2}, {512, 12, 4, 2, 2}, {384, 16, 4, 2, 2}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static const int g_variant[2] = {0, 2};  // [u32, u64]: measured best on GB300 without tuning
 static std::atomic<int> g_pinned[2] = {{-1}, {-1}};  // gtc_sort_set_variant: overrides the tuned choice
@@ -909,12 +948,12 @@ int sort_select_variant(int key_bits, int bits, uint32_t n) {
   return (t >= 0 && t < kNumVariants) ? t : g_variant[w];
 }
 
-template <class K, int THREADS, int KPT, bool HV, int MINB, bool EARLY, bool L2H = false>
+template <class K, int THREADS, int KPT, bool HV, int MINB, int RANK, bool L2H = false>
 static cudaError_t launch_one(const Launch& L, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
                               uint32_t n, int shift, uint32_t dmask, const uint32_t* bin_off, uint32_t* desc,
                               uint32_t* tile_counter) {
   using S = OnesweepSmem<K, THREADS, KPT>;
-  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, EARLY, L2H>;
+  auto kern = onesweep_kernel<K, THREADS, KPT, HV, MINB, 8, RANK, L2H>;
   cudaError_t e = kernel_setup(kern, THREADS, sizeof(S));
   if (e != cudaSuccess) return e;
   const uint32_t tiles = ceil_div(n, S::TILE);
@@ -945,32 +984,35 @@ static cudaError_t launch_variant(int v, bool hv, const Launch& L, const K* kin,
   // one-tile-per-CTA kernel of the same tile width.
   const bool aligned = (reinterpret_cast<uintptr_t>(kin) & 15) == 0 && (!hv || (reinterpret_cast<uintptr_t>(vin) & 15) == 0);
   if ((kVariants[v].kind == 1 || kVariants[v].kind == 2) && (!aligned || (hv && !vin))) v = 0;
-#define GTC_OS(T, P, MB, LB)                                                                                   \
-  return hv ? launch_one<K, T, P, true, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
-            : launch_one<K, T, P, false, MB, LB>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
-#define GTC_OSH(T, P, MB, EA)                                                                                  \
-  return hv ? launch_one<K, T, P, true, MB, EA, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
-            : launch_one<K, T, P, false, MB, EA, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_OS(T, P, MB, RK)                                                                                   \
+  return hv ? launch_one<K, T, P, true, MB, RK>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
+            : launch_one<K, T, P, false, MB, RK>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
+#define GTC_OSH(T, P, MB, RK)                                                                                  \
+  return hv ? launch_one<K, T, P, true, MB, RK, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc) \
+            : launch_one<K, T, P, false, MB, RK, true>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
 #define GTC_TMA(T, P, M)                                                                                     \
   return hv ? launch_tma<K, T, P, true, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)    \
             : launch_tma<K, T, P, false, M>(L, kin, vin, kout, vout, n, shift, dmask, bin_off, desc, tc)
   switch (v) {
-    case 0: GTC_OS(256, 16, 3, true);
-    case 1: GTC_OS(384, 16, 2, true);
-    case 2: GTC_OS(512, 12, 2, true);
+    case 0: GTC_OS(256, 16, 3, 0);
+    case 1: GTC_OS(384, 16, 2, 0);
+    case 2: GTC_OS(512, 12, 2, 0);
     case 3: GTC_TMA(256, 16, true);
     case 4: GTC_TMA(256, 16, false);
     case 5: GTC_TMA(512, 8, false);
     case 6: GTC_TMA(256, 24, false);
-    case 7: GTC_OS(256, 16, 4, true);
-    case 8: GTC_OS(512, 8, 2, true);
-    case 9: GTC_OS(384, 12, 3, true);
-    case 10: GTC_OS(256, 16, 3, false);
-    case 11: GTC_OS(384, 16, 2, false);
-    case 12: GTC_OS(512, 12, 2, false);
-    case 13: GTC_OS(256, 24, 2, false);
-    case 14: GTC_OSH(256, 16, 3, true);
-    default: GTC_OSH(512, 12, 2, false);
+    case 7: GTC_OS(256, 16, 4, 0);
+    case 8: GTC_OS(512, 8, 2, 0);
+    case 9: GTC_OS(384, 12, 3, 0);
+    case 10: GTC_OS(256, 16, 3, 1);
+    case 11: GTC_OS(384, 16, 2, 1);
+    case 12: GTC_OS(512, 12, 2, 1);
+    case 13: GTC_OS(256, 24, 2, 1);
+    case 14: GTC_OSH(256, 16, 3, 0);
+    case 15: GTC_OSH(512, 12, 2, 1);
+    case 16: GTC_OSH(256, 16, 3, 2);
+    case 17: GTC_OSH(512, 12, 2, 2);
+    default: GTC_OSH(384, 16, 2, 2);
   }
 #undef GTC_OS
 #undef GTC_OSH
