@@ -49,6 +49,7 @@ constexpr int LC_ILP = 4;          // keys per thread searched at once (independ
 constexpr int BS_THREADS = 512;    // in-bucket sort: two CTAs per SM
 constexpr int BS_CAP = 8192;       // keys per bucket sorted on chip
 constexpr int BS_IPT = BS_CAP / BS_THREADS;
+constexpr int kFallbackVariant = 4;  // onesweep variant of the fallback: persistent, TMA-fed
 constexpr int MAX_BUCKETS = 16384;  // the Eytzinger knots + bucket histogram fill one CTA's shared memory
 
 // ---------------------------------------------------------------- model ---
@@ -499,6 +500,7 @@ __device__ __forceinline__ uint32_t half16(uint32_t word, uint32_t d) { return (
 // halves never carry: every count and offset is below BS_CAP) and a second
 // sweep scatters the indices.  A digit shared by every key makes the pass the
 // identity: skipped.  Called by every thread of the block.
+template <int IPT>
 __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt, int shift, int& cur,
                                             const uint64_t* gkeys) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -512,10 +514,10 @@ __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt
   const uint32_t sel = 0x4440u + (uint32_t)(shift >> 3);  // byte select of the sort word
   // Per key: rank within the warp's digit run (< 32 * BS_IPT = 512: 9 bits) |
   // digit << 9 | moving index << 17 (< BS_CAP: 13 bits); ~0: no key.
-  static_assert(32 * BS_IPT <= 512 && BS_CAP <= 8192, "rank, digit and index pack into 30 bits");
-  uint32_t rk[BS_IPT];
+  static_assert(32 * IPT <= 512 && BS_CAP <= 8192, "rank, digit and index pack into 30 bits");
+  uint32_t rk[IPT];
 #pragma unroll
-  for (int j = 0; j < BS_IPT; ++j) {
+  for (int j = 0; j < IPT; ++j) {
     rk[j] = 0xffffffffu;
     if (j < ipt && wrun + j * 32 < cnt) {  // warp-uniform
       const uint32_t pos = wrun + j * 32 + lane;
@@ -589,7 +591,7 @@ __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt
   }
   __syncthreads();
 #pragma unroll
-  for (int j = 0; j < BS_IPT; ++j) {
+  for (int j = 0; j < IPT; ++j) {
     if (rk[j] != 0xffffffffu) {
       const uint32_t d = (rk[j] >> 9) & 255u;
       s.idx[cur ^ 1][half16(row[d >> 1], d) + (rk[j] & 511u)] = (uint16_t)(rk[j] >> 17);
@@ -597,6 +599,49 @@ __device__ __forceinline__ void bucket_pass(BucketSmem& s, uint32_t cnt, int ipt
   }
   __syncthreads();
   cur ^= 1;
+}
+
+// The passes and the run fixup of one bucket (see bucket_sort_kernel), the
+// pass loops unrolled for IPT keys per thread.  Returns the index array
+// holding the final order.
+template <int IPT>
+__device__ __forceinline__ int bucket_sort_body(BucketSmem& s, uint32_t cnt, int ipt, int vbits,
+                                                const uint64_t* keys) {
+  const int tid = threadIdx.x;
+  int cur = 0;
+  const int np = (min(vbits, BS_SORT_BITS) + 7) / 8;
+  for (int p = 0; p < np; ++p) bucket_pass<IPT>(s, cnt, ipt, 8 * p, cur, nullptr);
+  if (vbits > BS_SORT_BITS) {
+    uint16_t* ix = s.idx[cur];
+    for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+      const uint32_t h = s.sk[ix[i]];
+      if (i > 0 && s.sk[ix[i - 1]] == h) continue;  // not a run start
+      uint32_t e = i + 1;
+      while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && s.sk[ix[e]] == h) ++e;
+      if (e - i > (uint32_t)BS_RUN_LIMIT) {
+        s.big = 1;
+        continue;
+      }
+      for (uint32_t a = i + 1; a < e; ++a) {  // stable: only strictly greater keys move up
+        const uint16_t x = ix[a];
+        const uint64_t kx = keys[x];
+        uint32_t c = a;
+        while (c > i && keys[ix[c - 1]] > kx) {
+          ix[c] = ix[c - 1];
+          --c;
+        }
+        ix[c] = x;
+      }
+    }
+    __syncthreads();
+    if (s.big) {  // block-uniform: start over with full passes over every varying bit
+      for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[0][i] = (uint16_t)i;
+      cur = 0;
+      __syncthreads();
+      for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass<IPT>(s, cnt, ipt, 8 * p, cur, keys);
+    }
+  }
+  return cur;
 }
 
 // One CTA per bucket.  Stable counting passes over the sort word (the 24
@@ -629,6 +674,10 @@ __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
     return;
   }
   const uint64_t* keys = ukeys + off;
+  // The values are read once, gathered by the final order: request their
+  // lines into L2 now, so that the gather at the end does not wait on DRAM.
+  for (uint32_t i = tid * 32; i < cnt; i += BS_THREADS * 32) prefetch_l2(uvals + off + i);
+  if (tid == 0) prefetch_l2(uvals + off + cnt - 1);
   uint64_t mn = ~0ull, mx = 0;
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
     const uint64_t k = keys[i];
@@ -661,39 +710,10 @@ __global__ void __launch_bounds__(BS_THREADS, 2) bucket_sort_kernel(
   }
   __syncthreads();
   const int ipt = (int)((cnt + BS_THREADS - 1) / BS_THREADS);
-  int cur = 0;
-  const int np = (min(vbits, BS_SORT_BITS) + 7) / 8;
-  for (int p = 0; p < np; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur, nullptr);
-  if (vbits > BS_SORT_BITS) {
-    uint16_t* ix = s.idx[cur];
-    for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
-      const uint32_t h = s.sk[ix[i]];
-      if (i > 0 && s.sk[ix[i - 1]] == h) continue;  // not a run start
-      uint32_t e = i + 1;
-      while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && s.sk[ix[e]] == h) ++e;
-      if (e - i > (uint32_t)BS_RUN_LIMIT) {
-        s.big = 1;
-        continue;
-      }
-      for (uint32_t a = i + 1; a < e; ++a) {  // stable: only strictly greater keys move up
-        const uint16_t x = ix[a];
-        const uint64_t kx = keys[x];
-        uint32_t c = a;
-        while (c > i && keys[ix[c - 1]] > kx) {
-          ix[c] = ix[c - 1];
-          --c;
-        }
-        ix[c] = x;
-      }
-    }
-    __syncthreads();
-    if (s.big) {  // block-uniform: start over with full passes over every varying bit
-      for (uint32_t i = tid; i < cnt; i += BS_THREADS) s.idx[0][i] = (uint16_t)i;
-      cur = 0;
-      __syncthreads();
-      for (int p = 0; p < (vbits + 7) / 8; ++p) bucket_pass(s, cnt, ipt, 8 * p, cur, keys);
-    }
-  }
+  // passes unrolled for the bucket's keys per thread: 8, 12 or 16
+  const int cur = ipt <= 8    ? bucket_sort_body<8>(s, cnt, ipt, vbits, keys)
+                  : ipt <= 12 ? bucket_sort_body<12>(s, cnt, ipt, vbits, keys)
+                              : bucket_sort_body<BS_IPT>(s, cnt, ipt, vbits, keys);
   for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
     const uint16_t x = s.idx[cur][i];
     out_keys[off + i] = keys[x];
@@ -808,7 +828,7 @@ gtc_status cuda_fail(gtc_ctx* ctx, const char* what, cudaError_t e) {
   } while (0)
 
 // Count kernel: Eytzinger knots + per-bucket counters.
-size_t count_smem_bytes(int B) { return (size_t)B * 8 + (size_t)B * 4; }
+size_t count_smem_bytes(int B) { return (size_t)B * 12; }
 
 // Derives the sort-time model arrays from the knots and heights.
 gtc_status prepare_model(gtc_ctx* ctx, const gtc_learned_model* m, uint32_t* d_flags, cudaStream_t s) {
@@ -1002,15 +1022,18 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
   learned_order_check_kernel<<<ceil_div(B, 256), 256, 0, s>>>(W.totals, W.bmin, W.bmax, B, d_flags);
   LTRY(ctx, cudaGetLastError());
   // Fallback: copy + plain onesweep, all gated on the flag word.
-  cond_copy_kernel<<<L0.num_sms * 8, 256, 0, s>>>(keys, vals, keys_out, vals_out, n, d_flags);
+  cond_copy_kernel<<<L0.num_sms * 4, 256, 0, s>>>(keys, vals, keys_out, vals_out, n, d_flags);
   Launch L = L0;
   L.run_if = d_flags;
   const SortWorkspace SW = carve_sort_workspace(W.sort_ws, n, 8, 0);
   LTRY(ctx, cudaMemsetAsync(SW.header, 0, SW.header_words * 4, s));
   LTRY(ctx, launch_global_hist<uint64_t>(L, keys_out, n, 0, 64, SW, 8));
   bool in_alt = false;
+  // Variant 4 is a persistent kernel (one resident wave of CTAs pulling
+  // tiles): when the learned path succeeded, each gated pass costs one wave
+  // of CTAs that read the flag word and exit, not one CTA per tile.
   LTRY(ctx, launch_onesweep_passes<uint64_t>(L, keys_out, vals_out, W.tkeys, W.tvals, n, 0, 64, SW, 8, &in_alt,
-                                             nullptr));
+                                             nullptr, kFallbackVariant));
   return GTC_OK;
 }
 
