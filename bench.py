@@ -464,6 +464,8 @@ def measure_batched(ctx, S, steps, warmup, seed=0, pts_np=None, offs_np=None):
     pts = torch.from_numpy(pts_np).cuda()
     offs = torch.from_numpy(offs_np.view(np.int32)).cuda()
     plan = gtc.BatchPlan(ctx, n, S, nodes_capacity=n + (n >> 1) + S)
+    # the autotuner's pick of the segmented onesweep's tile shape for this batch
+    tune = plan.autotune(pts, offs, reps=2)
     for _ in range(max(warmup, 3)):
         plan.launch(pts, offs)
     torch.cuda.synchronize()
@@ -485,7 +487,8 @@ def measure_batched(ctx, S, steps, warmup, seed=0, pts_np=None, offs_np=None):
     graph_ms = events_ms(stream, plan.replay, steps)
     ctx.device_status()
     return dict(plan=plan, pts=pts, offs=offs, pts_np=pts_np, offs_np=offs_np, n=n, u=u, m=m, o=o,
-                eager_ms=eager_ms, graph_ms=graph_ms, stages=stages)
+                eager_ms=eager_ms, graph_ms=graph_ms, stages=stages, variant=tune["best"],
+                tune_ms=[round(t, 4) for t in tune["ms"]])
 
 
 # ----------------------------------------------------------------- gtc ----
@@ -686,7 +689,8 @@ def measure_forms(ctx, args):
     b = measure_batched(ctx, 512, steps, 3)
     forms["batched_512_clouds"] = {
         "mpoints_s": round(b["n"] / (b["graph_ms"] * 1e-3) / 1e6, 1), "ms": round(b["graph_ms"], 4),
-        "n_points": b["n"], "eager_ms": round(b["eager_ms"], 4),
+        "n_points": b["n"], "eager_ms": round(b["eager_ms"], 4), "batched_variant": b["variant"],
+        "autotune_batched_ms": b["tune_ms"],
         "stage_ms": {k: round(v[0] / steps, 4) for k, v in b["stages"].items() if v[1]}}
     del b
     torch.cuda.empty_cache()
@@ -937,6 +941,7 @@ def run_gtc_batched(args):
                     "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (points alone exceed 1 GB)",
                     "timing": "CUDA-graph replay of the whole batch per step",
                     "eager_ms_per_step": round(b["eager_ms"], 4), "stage_ms_per_step": stage_ms,
+                    "batched_variant": b["variant"], "autotune_batched_ms": b["tune_ms"],
                     "algorithmic_GB_per_step": round(alg_total / 1e9, 4),
                     "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4)},
         "roofline": {"bound": "hbm", "kernel": "bt_onesweep_kernel (one segmented 8-bit pass, u32 key + u32 value)",

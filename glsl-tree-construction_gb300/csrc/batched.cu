@@ -26,6 +26,7 @@
 //   7. octree of each cloud (octree_warp_batch) into its node range starting
 //               at O_c = (non-empty clouds before c) + bias.
 
+#include <atomic>
 #include <utility>
 
 #include "karras.cuh"
@@ -54,10 +55,18 @@ struct Stage {
 
 constexpr int BRADIX = 256;
 constexpr int BPASSES = 4;  // 30-bit codes in 8-bit digits
-constexpr int BT_THREADS = 512;
-constexpr int BT_KPT = 12;
-constexpr int BT_TILE = BT_THREADS * BT_KPT;  // 6144 keys
-constexpr int BT_WARPS = BT_THREADS / 32;
+constexpr int BM_THREADS = 512;  // Morton kernel: one block per tile
+// Segmented onesweep tile shapes (threads x keys per thread), compiled as
+// variants: pinned with gtc_batched_set_variant, else the autotuner's pick
+// for the batch's size (gtc_autotune_batched), else variant 0.  Every tile
+// division of the batch (tile list, Morton blocks, sort tiles) uses the
+// chosen shape's tile.
+struct BtVariant {
+  int threads, kpt;
+};
+constexpr BtVariant kBtVariants[] = {{512, 12}, {256, 16}, {384, 16}, {512, 8}, {256, 24}};
+constexpr int kBtNumVariants = sizeof(kBtVariants) / sizeof(kBtVariants[0]);
+constexpr uint32_t BT_MIN_TILE = 4096;  // smallest tile of any variant: sizes the workspace
 constexpr int BU_THREADS = 512;
 constexpr int BU_IPT = 9;
 constexpr int BU_TILE = BU_THREADS * BU_IPT;  // the scan tile of scan.cu
@@ -67,7 +76,7 @@ constexpr uint32_t MAX_CLOUDS = 1u << 20;
 // offsets must partition [0, n): off[0] = 0, non-decreasing, off[S] = n.
 // Otherwise the batch is flagged bad, every later kernel returns at once and
 // the outputs say zero unique codes and zero nodes.
-__global__ void __launch_bounds__(1024) bt_tiles_kernel(const uint32_t* off, uint32_t S, uint32_t n,
+__global__ void __launch_bounds__(1024) bt_tiles_kernel(const uint32_t* off, uint32_t S, uint32_t n, uint32_t tile,
                                                         uint32_t* tile_start, uint32_t* ne_start, uint32_t* bad,
                                                         uint32_t* uoff, uint32_t* status) {
   __shared__ uint32_t s_t[1024], s_n[1024];
@@ -87,7 +96,7 @@ __global__ void __launch_bounds__(1024) bt_tiles_kernel(const uint32_t* off, uin
   uint32_t t = 0, ne = 0;
   for (uint32_t c = first; c < last; ++c) {
     const uint32_t len = off[c + 1] - off[c];
-    t += (len + BT_TILE - 1) / BT_TILE;
+    t += (len + tile - 1) / tile;
     ne += len > 0;
   }
   s_t[threadIdx.x] = t;
@@ -107,7 +116,7 @@ __global__ void __launch_bounds__(1024) bt_tiles_kernel(const uint32_t* off, uin
     const uint32_t len = off[c + 1] - off[c];
     tile_start[c] = t;
     ne_start[c] = ne;
-    t += (len + BT_TILE - 1) / BT_TILE;
+    t += (len + tile - 1) / tile;
     ne += len > 0;
   }
   if (threadIdx.x == 1023) {
@@ -121,31 +130,32 @@ struct TileRange {
 };
 
 __device__ __forceinline__ TileRange tile_range(uint32_t t, const uint32_t* tile_start, const uint32_t* off,
-                                                uint32_t S) {
+                                                uint32_t S, uint32_t tile) {
   TileRange r;
   r.cloud = owner(tile_start, S, t);
   r.local = t - tile_start[r.cloud];
-  r.base = off[r.cloud] + r.local * BT_TILE;
-  r.valid = min((uint32_t)BT_TILE, off[r.cloud + 1] - r.base);
+  r.base = off[r.cloud] + r.local * tile;
+  r.valid = min(tile, off[r.cloud + 1] - r.base);
   return r;
 }
 
 // Morton codes (10 bits per axis), cloud-local payload, per-cloud digit
 // histograms; also clears the look-back descriptors of all passes.
-__global__ void __launch_bounds__(BT_THREADS) bt_morton_kernel(const float4* __restrict__ pts, const uint32_t* off,
-                                                               uint32_t S, const uint32_t* tile_start, float mn,
+__global__ void __launch_bounds__(BM_THREADS) bt_morton_kernel(const float4* __restrict__ pts, const uint32_t* off,
+                                                               uint32_t S, const uint32_t* tile_start, uint32_t tile,
+                                                               float mn,
                                                                float rg, float inv_rg, uint32_t* __restrict__ keys,
                                                                uint32_t* __restrict__ idx, uint32_t* seg_hist,
                                                                uint32_t* desc, size_t desc_words) {
   __shared__ uint32_t s_hist[BPASSES * BRADIX];
-  for (int i = threadIdx.x; i < BPASSES * BRADIX; i += BT_THREADS) s_hist[i] = 0;
-  const size_t stride = (size_t)gridDim.x * BT_THREADS;
-  for (size_t i = (size_t)blockIdx.x * BT_THREADS + threadIdx.x; i < desc_words; i += stride) desc[i] = 0;
+  for (int i = threadIdx.x; i < BPASSES * BRADIX; i += BM_THREADS) s_hist[i] = 0;
+  const size_t stride = (size_t)gridDim.x * BM_THREADS;
+  for (size_t i = (size_t)blockIdx.x * BM_THREADS + threadIdx.x; i < desc_words; i += stride) desc[i] = 0;
   __syncthreads();
   if (blockIdx.x >= tile_start[S]) return;
-  const TileRange r = tile_range(blockIdx.x, tile_start, off, S);
+  const TileRange r = tile_range(blockIdx.x, tile_start, off, S, tile);
   const uint32_t first = off[r.cloud];
-  for (uint32_t i = threadIdx.x; i < r.valid; i += BT_THREADS) {
+  for (uint32_t i = threadIdx.x; i < r.valid; i += BM_THREADS) {
     const uint32_t g = r.base + i;
     const uint32_t k = encode_point<uint32_t>(__ldcs(pts + g), mn, rg, inv_rg);
     keys[g] = k;
@@ -155,7 +165,7 @@ __global__ void __launch_bounds__(BT_THREADS) bt_morton_kernel(const float4* __r
   }
   __syncthreads();
   uint32_t* h = seg_hist + (size_t)r.cloud * BPASSES * BRADIX;
-  for (int i = threadIdx.x; i < BPASSES * BRADIX; i += BT_THREADS) {
+  for (int i = threadIdx.x; i < BPASSES * BRADIX; i += BM_THREADS) {
     const uint32_t c = s_hist[i];
     if (c) atomicAdd(h + i, c);
   }
@@ -179,12 +189,15 @@ __global__ void __launch_bounds__(BRADIX) bt_seg_scan_kernel(uint32_t* seg_hist,
   }
 }
 
+template <int THREADS, int KPT>
 struct BtSmem {
-  uint32_t keys[BT_TILE];
-  uint32_t vals[BT_TILE];
-  uint32_t warp_hist[BT_WARPS][BRADIX];
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int TILE = THREADS * KPT;
+  uint32_t keys[TILE];
+  uint32_t vals[TILE];
+  uint32_t warp_hist[WARPS][BRADIX];
   uint32_t gbase[BRADIX];
-  uint32_t warp_sums[BT_WARPS + 1];
+  uint32_t warp_sums[WARPS + 1];
   uint32_t tile_id;
 };
 
@@ -193,35 +206,39 @@ struct BtSmem {
 // cloud's last tile is padded with all-ones keys, which rank last in the tile
 // and are never stored.  Its descriptor counts them, but no tile reads it:
 // the next tile starts another cloud and does not look back.
-__global__ void __launch_bounds__(BT_THREADS) bt_onesweep_kernel(const uint32_t* __restrict__ kin,
+template <int THREADS, int KPT>
+__global__ void __launch_bounds__(THREADS) bt_onesweep_kernel(const uint32_t* __restrict__ kin,
                                                                  const uint32_t* __restrict__ vin,
                                                                  uint32_t* __restrict__ kout,
                                                                  uint32_t* __restrict__ vout, const uint32_t* off,
                                                                  uint32_t S, const uint32_t* tile_start, int shift,
                                                                  const uint32_t* seg_base, int pass, uint32_t* desc,
                                                                  uint32_t* tile_counter, uint32_t* status) {
+  using Sm = BtSmem<THREADS, KPT>;
+  constexpr int WARPS = Sm::WARPS;
+  static_assert(THREADS >= BRADIX, "one thread per digit");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  BtSmem& s = *reinterpret_cast<BtSmem*>(smem_raw);
+  Sm& s = *reinterpret_cast<Sm*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  for (int i = tid; i < BT_WARPS * BRADIX; i += BT_THREADS) (&s.warp_hist[0][0])[i] = 0;
+  for (int i = tid; i < WARPS * BRADIX; i += THREADS) (&s.warp_hist[0][0])[i] = 0;
   if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const uint32_t tile = s.tile_id;
   if (tile >= tile_start[S]) return;
-  const TileRange r = tile_range(tile, tile_start, off, S);
+  const TileRange r = tile_range(tile, tile_start, off, S, Sm::TILE);
 
-  uint32_t key[BT_KPT], val[BT_KPT];
-  const uint32_t wbase = warp * 32 * BT_KPT + lane;
+  uint32_t key[KPT], val[KPT];
+  const uint32_t wbase = warp * 32 * KPT + lane;
 #pragma unroll
-  for (int j = 0; j < BT_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t i = wbase + j * 32;
     key[j] = (i < r.valid) ? kin[r.base + i] : 0xffffffffu;
     val[j] = (i < r.valid) ? vin[r.base + i] : 0u;
   }
   uint32_t* my_hist = s.warp_hist[warp];
 #pragma unroll
-  for (int j = 0; j < BT_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (key[j] >> shift) & 255u;
     const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
     if (__all_sync(0xffffffffu, d == d0)) {
@@ -234,7 +251,7 @@ __global__ void __launch_bounds__(BT_THREADS) bt_onesweep_kernel(const uint32_t*
   uint32_t count = 0;
   if (tid < BRADIX) {
 #pragma unroll
-    for (int w = 0; w < BT_WARPS; ++w) {
+    for (int w = 0; w < WARPS; ++w) {
       const uint32_t c = s.warp_hist[w][tid];
       s.warp_hist[w][tid] = count;
       count += c;
@@ -243,14 +260,14 @@ __global__ void __launch_bounds__(BT_THREADS) bt_onesweep_kernel(const uint32_t*
   }
   // Exclusive scan of the 256 digit counts (threads past 256 add zeros).
   uint32_t total;
-  const uint32_t doff = block_exclusive<BT_THREADS>(tid < BRADIX ? count : 0u, s.warp_sums, &total);
+  const uint32_t doff = block_exclusive<THREADS>(tid < BRADIX ? count : 0u, s.warp_sums, &total);
   if (tid < BRADIX) {
 #pragma unroll
-    for (int w = 0; w < BT_WARPS; ++w) s.warp_hist[w][tid] += doff;
+    for (int w = 0; w < WARPS; ++w) s.warp_hist[w][tid] += doff;
   }
   __syncthreads();
 #pragma unroll
-  for (int j = 0; j < BT_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (key[j] >> shift) & 255u;
     uint32_t peers = 0xffffffffu;
 #pragma unroll
@@ -276,7 +293,7 @@ __global__ void __launch_bounds__(BT_THREADS) bt_onesweep_kernel(const uint32_t*
     s.gbase[tid] = seg_base[((size_t)r.cloud * BPASSES + pass) * BRADIX + tid] + excl - doff;
   }
   __syncthreads();
-  for (uint32_t i = tid; i < r.valid; i += BT_THREADS) {
+  for (uint32_t i = tid; i < r.valid; i += THREADS) {
     const uint32_t k = s.keys[i];
     const uint32_t o = s.gbase[(k >> shift) & 255u] + i;
     kout[o] = k;
@@ -603,6 +620,38 @@ __global__ void __launch_bounds__(BT_OCT_THREADS) bt_octree_kernel(const uint32_
   if (qn > 0) run_batch(qn);
 }
 
+template <int THREADS, int KPT>
+cudaError_t launch_bt_pass(cudaStream_t s, uint32_t grid, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                           uint32_t* vout, const uint32_t* off, uint32_t S, const uint32_t* tile_start, int shift,
+                           const uint32_t* seg_base, int pass, uint32_t* desc, uint32_t* tile_counter,
+                           uint32_t* status) {
+  using Sm = BtSmem<THREADS, KPT>;
+  cudaError_t e = kernel_setup(bt_onesweep_kernel<THREADS, KPT>, THREADS, sizeof(Sm));
+  if (e != cudaSuccess) return e;
+  bt_onesweep_kernel<THREADS, KPT><<<grid, THREADS, sizeof(Sm), s>>>(kin, vin, kout, vout, off, S, tile_start, shift,
+                                                                     seg_base, pass, desc, tile_counter, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bt_variant(int v, cudaStream_t s, uint32_t grid, const uint32_t* kin, const uint32_t* vin,
+                              uint32_t* kout, uint32_t* vout, const uint32_t* off, uint32_t S,
+                              const uint32_t* tile_start, int shift, const uint32_t* seg_base, int pass,
+                              uint32_t* desc, uint32_t* tile_counter, uint32_t* status) {
+#define GTC_BT(T, K)                                                                                               \
+  return launch_bt_pass<T, K>(s, grid, kin, vin, kout, vout, off, S, tile_start, shift, seg_base, pass, desc, \
+                              tile_counter, status)
+  switch (v) {
+    case 1: GTC_BT(256, 16);
+    case 2: GTC_BT(384, 16);
+    case 3: GTC_BT(512, 8);
+    case 4: GTC_BT(256, 24);
+    default: GTC_BT(512, 12);
+  }
+#undef GTC_BT
+}
+
+std::atomic<int> g_bt_pinned{-1};  // gtc_batched_set_variant
+
 struct BatchWs {
   uint32_t* tile_start;  // [S + 1]
   uint32_t* ne_start;    // [S + 1]
@@ -618,9 +667,9 @@ struct BatchWs {
 };
 
 // A cloud of len points has ceil(len / TILE) tiles, so the batch has at most
-// n / TILE + S of them.
+// n / TILE + S of them; sized for the smallest tile of any variant.
 size_t batch_layout(uint32_t n, uint32_t S, BatchWs* W, char* p) {
-  const uint32_t tiles_max = ceil_div(n > 0 ? n : 1, BT_TILE) + S;
+  const uint32_t tiles_max = ceil_div(n > 0 ? n : 1, BT_MIN_TILE) + S;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     char* q = p ? p + o : nullptr;
@@ -656,11 +705,26 @@ GTC_API gtc_status gtc_batched_workspace_size(uint32_t n_total, uint32_t n_cloud
   return GTC_OK;
 }
 
-GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,
-                                            uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
-                                            const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
-                                            gtc_stream_t stream) {
+}  // extern "C"
+
+namespace gtc {
+int batched_select_variant(uint32_t n) {
+  const int pinned = g_bt_pinned.load(std::memory_order_relaxed);
+  if (pinned >= 0) return pinned;
+  const int t = tuned_batched_variant(n);
+  return (t >= 0 && t < kBtNumVariants) ? t : 0;
+}
+int batched_num_variants() { return kBtNumVariants; }
+
+// The batched build with the segmented onesweep's tile shape given.
+gtc_status build_octree_batched_variant(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,
+                                        uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
+                                        const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
+                                        gtc_stream_t stream, int variant) {
   if (!ctx) return GTC_ERR_INVALID_ARG;
+  if (variant < 0 || variant >= kBtNumVariants)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "no such batched variant", cudaSuccess);
+  const uint32_t tile = (uint32_t)(kBtVariants[variant].threads * kBtVariants[variant].kpt);
   if (!out || !d_offsets || n_clouds == 0 || n_clouds > MAX_CLOUDS)
     return context_error(ctx, GTC_ERR_INVALID_ARG, "need offsets, outputs and 1..2^20 clouds", cudaSuccess);
   if (n_total >= (1u << 30)) return context_error(ctx, GTC_ERR_INVALID_ARG, "n_total must be < 2^30", cudaSuccess);
@@ -684,7 +748,6 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   do {                                                                            \
     if ((e = (x)) != cudaSuccess) return context_error(ctx, GTC_ERR_CUDA, #x, e); \
   } while (0)
-  BCHK(kernel_setup(bt_onesweep_kernel, BT_THREADS, sizeof(BtSmem)));
   if (n_total == 0) {
     BCHK(cudaMemsetAsync(out->key_offset, 0, ((size_t)S + 1) * 4, s));
     BCHK(cudaMemsetAsync(out->node_offset, 0, ((size_t)S + 1) * 4, s));
@@ -696,11 +759,11 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
     Stage t(ctx, stream, GTC_STAGE_MORTON);
     BCHK(cudaMemsetAsync(W.seg_hist, 0, (size_t)S * BPASSES * BRADIX * 4, s));
     BCHK(cudaMemsetAsync(W.counters, 0, 256, s));
-    bt_tiles_kernel<<<1, 1024, 0, s>>>(d_offsets, S, n_total, W.tile_start, W.ne_start, bad, out->key_offset,
-                                       L.status);
+    bt_tiles_kernel<<<1, 1024, 0, s>>>(d_offsets, S, n_total, tile, W.tile_start, W.ne_start, bad,
+                                       out->key_offset, L.status);
     BCHK(cudaGetLastError());
-    bt_morton_kernel<<<W.tiles_max, BT_THREADS, 0, s>>>(reinterpret_cast<const float4*>(pts), d_offsets, S,
-                                                        W.tile_start, min_coord, range, pow2_reciprocal(range),
+    bt_morton_kernel<<<W.tiles_max, BM_THREADS, 0, s>>>(reinterpret_cast<const float4*>(pts), d_offsets, S,
+                                                        W.tile_start, tile, min_coord, range, pow2_reciprocal(range),
                                                         W.keys_alt, W.idx_alt,
                                                         W.seg_hist, W.desc, W.desc_words);
     BCHK(cudaGetLastError());
@@ -713,10 +776,8 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
   uint32_t* dst_v = out->idx;
   for (int p = 0; p < BPASSES; ++p) {
     Stage t(ctx, stream, GTC_STAGE_ONESWEEP);
-    bt_onesweep_kernel<<<W.tiles_max, BT_THREADS, sizeof(BtSmem), s>>>(
-        src_k, src_v, dst_k, dst_v, d_offsets, S, W.tile_start, 8 * p, W.seg_hist, p,
-        W.desc + (size_t)p * W.tiles_max * BRADIX, W.counters + p, L.status);
-    BCHK(cudaGetLastError());
+    BCHK(launch_bt_variant(variant, s, W.tiles_max, src_k, src_v, dst_k, dst_v, d_offsets, S, W.tile_start, 8 * p,
+                           W.seg_hist, p, W.desc + (size_t)p * W.tiles_max * BRADIX, W.counters + p, L.status));
     std::swap(src_k, dst_k);
     std::swap(src_v, dst_v);
   }
@@ -792,5 +853,33 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
 #undef BCHK
   return GTC_OK;
 }
+}  // namespace gtc
+
+extern "C" {
+
+GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,
+                                            uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
+                                            const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
+                                            gtc_stream_t stream) {
+  return build_octree_batched_variant(ctx, pts, d_offsets, n_clouds, n_total, min_coord, range, out, ws, ws_bytes,
+                                      stream, batched_select_variant(n_total));
+}
+
+GTC_API int gtc_batched_num_variants(void) { return kBtNumVariants; }
+
+GTC_API gtc_status gtc_batched_variant_shape(int variant, int* threads, int* keys_per_thread) {
+  if (variant < 0 || variant >= kBtNumVariants) return GTC_ERR_INVALID_ARG;
+  if (threads) *threads = kBtVariants[variant].threads;
+  if (keys_per_thread) *keys_per_thread = kBtVariants[variant].kpt;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_batched_set_variant(int variant) {
+  if (variant < -1 || variant >= kBtNumVariants) return GTC_ERR_INVALID_ARG;
+  g_bt_pinned.store(variant, std::memory_order_relaxed);
+  return GTC_OK;
+}
+
+GTC_API int gtc_batched_get_variant(uint32_t n_total) { return batched_select_variant(n_total); }
 
 }  // extern "C"

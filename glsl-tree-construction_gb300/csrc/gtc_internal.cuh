@@ -498,6 +498,14 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
 int sort_select_variant(int key_bits, int bits, uint32_t n);
 // Autotuner cache (tune.cu): the tuned variant for (key width, bits, n), or -1.
 int tuned_variant(int key_bits, int bits, uint32_t n);
+// The tuned batched onesweep shape for a batch of n points, or -1 (tune.cu).
+int tuned_batched_variant(uint32_t n);
+// The batched build with the segmented onesweep shape given (batched.cu).
+int batched_num_variants();
+gtc_status build_octree_batched_variant(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,
+                                        uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
+                                        const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
+                                        gtc_stream_t stream, int variant);
 
 // Decoupled look-back scans: unique compaction and node offsets.
 size_t scan_workspace_bytes(uint32_t n);

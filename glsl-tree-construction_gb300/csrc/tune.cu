@@ -42,6 +42,11 @@ struct TuneEntry {
 
 std::mutex g_mu;
 std::map<TuneKey, TuneEntry> g_cache;
+// Other tuned shapes by (kind, ceil(log2 n)): the batched build's segmented
+// onesweep (kind "batched").
+enum TuneKind { TK_BATCHED = 0 };
+const char* const kKindName[] = {"batched"};
+std::map<std::pair<int, int>, TuneEntry> g_xcache;
 bool g_env_loaded = false;
 
 int log2_bucket(uint32_t n) {
@@ -60,6 +65,9 @@ bool load_locked(const char* path) {
     if (sscanf(line, "sort %d %d %d %d %f", &kb, &bits, &lg, &v, &ms) == 5 && (kb == 32 || kb == 64) &&
         bits >= 1 && bits <= kb && lg >= 0 && lg <= 32 && v >= 0 && v < sort_num_variants())
       g_cache[TuneKey{kb, bits, lg}] = TuneEntry{v, ms};
+    else if (sscanf(line, "batched %d %d %f", &lg, &v, &ms) == 3 && lg >= 0 && lg <= 32 && v >= 0 &&
+             v < batched_num_variants())
+      g_xcache[{TK_BATCHED, lg}] = TuneEntry{v, ms};
   }
   fclose(f);
   return true;
@@ -68,10 +76,12 @@ bool load_locked(const char* path) {
 bool save_locked(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return false;
-  fprintf(f, "# gtc onesweep autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms>\n");
+  fprintf(f, "# gtc autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms> | batched <log2n> <variant> <ms>\n");
   for (const auto& kv : g_cache)
     fprintf(f, "sort %d %d %d %d %.6f\n", kv.first.key_bits, kv.first.bits, kv.first.log2n, kv.second.variant,
             kv.second.ms);
+  for (const auto& kv : g_xcache)
+    fprintf(f, "%s %d %d %.6f\n", kKindName[kv.first.first], kv.first.second, kv.second.variant, kv.second.ms);
   fclose(f);
   return true;
 }
@@ -193,6 +203,13 @@ int tuned_variant(int key_bits, int bits, uint32_t n) {
   return it == g_cache.end() ? -1 : it->second.variant;
 }
 
+int tuned_batched_variant(uint32_t n) {
+  std::lock_guard<std::mutex> g(g_mu);
+  load_env_once_locked();
+  const auto it = g_xcache.find({TK_BATCHED, log2_bucket(n)});
+  return it == g_xcache.end() ? -1 : it->second.variant;
+}
+
 }  // namespace gtc
 
 using namespace gtc;
@@ -226,14 +243,64 @@ GTC_API gtc_status gtc_autotune_clear(void) {
   std::lock_guard<std::mutex> g(g_mu);
   g_env_loaded = true;  // an explicit clear also drops the environment's file
   g_cache.clear();
+  g_xcache.clear();
   return GTC_OK;
 }
 
 GTC_API int gtc_autotune_entries(void) {
   std::lock_guard<std::mutex> g(g_mu);
   load_env_once_locked();
-  return (int)g_cache.size();
+  return (int)(g_cache.size() + g_xcache.size());
 }
+
+GTC_API gtc_status gtc_autotune_batched(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets, uint32_t n_clouds,
+                                        uint32_t n_total, float min_coord, float range, const gtc_batch_buffers* out,
+                                        void* ws, size_t ws_bytes, int reps, int* best_variant, float* times_ms) {
+  if (!ctx) return GTC_ERR_INVALID_ARG;
+  if (n_total == 0 || reps < 1 || reps > 100)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: need n_total > 0 and 1 <= reps <= 100", cudaSuccess);
+  const int nv = batched_num_variants();
+  std::vector<float> t(nv, FLT_MAX);
+  cudaStream_t s = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  gtc_status st = GTC_OK;
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess)
+    st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
+  gtc_stream_t gs = reinterpret_cast<gtc_stream_t>(s);
+  for (int vi = 0; vi < nv && st == GTC_OK; ++vi) {
+    for (int r = 0; r <= reps && st == GTC_OK; ++r) {  // r = 0 warms up (and sets kernel attributes)
+      cudaEventRecord(a, s);
+      st = build_octree_batched_variant(ctx, pts, d_offsets, n_clouds, n_total, min_coord, range, out, ws,
+                                        ws_bytes, gs, vi);
+      cudaEventRecord(b, s);
+      if (st == GTC_OK && (e = cudaEventSynchronize(b)) != cudaSuccess)
+        st = context_error(ctx, GTC_ERR_CUDA, "autotune: timed batched build", e);
+      float ms = 0.f;
+      if (st == GTC_OK && r > 0 && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < t[vi]) t[vi] = ms;
+    }
+  }
+  if (s) cudaStreamSynchronize(s);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (s) cudaStreamDestroy(s);
+  if (st != GTC_OK) return st;
+  int bv = 0;
+  for (int vi = 1; vi < nv; ++vi)
+    if (t[vi] < t[bv]) bv = vi;
+  if (best_variant) *best_variant = bv;
+  if (times_ms)
+    for (int vi = 0; vi < nv; ++vi) times_ms[vi] = t[vi];
+  std::lock_guard<std::mutex> g(g_mu);
+  load_env_once_locked();
+  g_xcache[{TK_BATCHED, log2_bucket(n_total)}] = TuneEntry{bv, t[bv]};
+  const char* p = getenv("GTC_TUNE_CACHE");
+  if (p && *p) save_locked(p);
+  return GTC_OK;
+}
+
+GTC_API int gtc_autotune_lookup_batched(uint32_t n_total) { return tuned_batched_variant(n_total); }
 
 GTC_API gtc_status gtc_autotune_save(const char* path) {
   if (!path) return GTC_ERR_INVALID_ARG;

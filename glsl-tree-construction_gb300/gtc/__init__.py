@@ -473,6 +473,22 @@ class BatchPlan:
             self.ctx.h, _ptr(pts), _ptr(offsets), n_clouds, n_total, min_coord, rng, ctypes.byref(self.bufs),
             _ptr(self.ws), self.ws.numel(), _stream(stream)))
 
+    def autotune(self, pts, offsets, n_total: int | None = None, min_coord=0.0, rng=1024.0, reps: int = 3) -> dict:
+        """Time every batched onesweep shape on this batch and cache the
+        fastest for its size; returns {"best": variant, "ms": [per-variant best
+        build time]}.  Leaves the outputs of the last timed build."""
+        n_clouds = offsets.shape[0] - 1
+        n_total = pts.shape[0] if n_total is None else n_total
+        assert 1 <= n_clouds <= self.clouds_max and n_total <= self.n_max
+        self.n_clouds = n_clouds
+        nv = self.ctx.L.gtc_batched_num_variants()
+        times = (ctypes.c_float * nv)()
+        best = ctypes.c_int(-1)
+        self.ctx.check(self.ctx.L.gtc_autotune_batched(
+            self.ctx.h, _ptr(pts), _ptr(offsets), n_clouds, n_total, min_coord, rng, ctypes.byref(self.bufs),
+            _ptr(self.ws), self.ws.numel(), reps, ctypes.byref(best), times))
+        return {"best": best.value, "ms": [float(t) for t in times]}
+
     def capture(self, pts, offsets, n_total: int | None = None, min_coord=0.0, rng=1024.0):
         """Capture the whole batched pipeline into one CUDA graph."""
         torch = _torch()
@@ -511,6 +527,32 @@ class BatchPlan:
                                    self.parent[k0:k0 + m], self.edge[k0:k0 + m], self.ps[k0:k0 + u],
                                    self.nodes[n0:n0 + o], u, m, o))
         return out
+
+
+def batched_variants() -> list:
+    """(threads, keys per thread) of every batched onesweep variant."""
+    L = lib()
+    out = []
+    for v in range(L.gtc_batched_num_variants()):
+        t, k = ctypes.c_int(), ctypes.c_int()
+        if L.gtc_batched_variant_shape(v, ctypes.byref(t), ctypes.byref(k)) != 0:
+            raise GtcError(1, "gtc_batched_variant_shape")
+        out.append((t.value, k.value))
+    return out
+
+
+def batched_set_variant(v: int):
+    """Pin one batched onesweep shape for every batched build (-1 unpins)."""
+    if lib().gtc_batched_set_variant(v) != 0:
+        raise GtcError(1, f"no batched variant {v}")
+
+
+def batched_get_variant(n_total: int) -> int:
+    return lib().gtc_batched_get_variant(n_total)
+
+
+def autotune_lookup_batched(n_total: int) -> int:
+    return lib().gtc_autotune_lookup_batched(n_total)
 
 
 def build_octree_batched(ctx: Context, pts, offsets, min_coord=0.0, rng=1024.0) -> list:

@@ -336,6 +336,17 @@ GTC_API gtc_status gtc_build_octree_batched(gtc_ctx* ctx, const float* pts, cons
                                             uint32_t n_clouds, uint32_t n_total, float min_coord, float range,
                                             const gtc_batch_buffers* out, void* ws, size_t ws_bytes,
                                             gtc_stream_t stream);
+/* Tile shapes of the batch's segmented onesweep compiled into the library
+ * (threads per block x keys per thread; the tile also divides the clouds for
+ * the Morton pass).  A build uses the pinned variant, else the autotuner's
+ * pick for its n_total (gtc_autotune_batched), else variant 0.  Every
+ * variant gives identical output.  No reference counterpart. */
+GTC_API int gtc_batched_num_variants(void);
+GTC_API gtc_status gtc_batched_variant_shape(int variant, int* threads, int* keys_per_thread);
+/* Pins one variant for every batched build; variant = -1 unpins. */
+GTC_API gtc_status gtc_batched_set_variant(int variant);
+/* The variant a batched build of n_total points uses now. */
+GTC_API int gtc_batched_get_variant(uint32_t n_total);
 
 /* The same sort of 32-bit keys (optionally with u32 values) for callers that
  * must not allocate device memory at the point where they sort: cudaMalloc /
@@ -436,6 +447,16 @@ GTC_API int gtc_autotune_lookup(int key_bits, int bits, uint32_t n);
 GTC_API gtc_status gtc_autotune_record(int key_bits, int bits, uint32_t n, int variant, float ms);
 GTC_API gtc_status gtc_autotune_clear(void);
 GTC_API int gtc_autotune_entries(void);
+/* Times every batched variant on the caller's own batch: `reps` timed builds
+ * after one warm-up each, through the caller's outputs and workspace
+ * (arguments as gtc_build_octree_batched), and caches the fastest for
+ * ceil(log2 n_total).  best_variant and times_ms[gtc_batched_num_variants()]
+ * are nullable.  Synchronous. */
+GTC_API gtc_status gtc_autotune_batched(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets, uint32_t n_clouds,
+                                        uint32_t n_total, float min_coord, float range, const gtc_batch_buffers* out,
+                                        void* ws, size_t ws_bytes, int reps, int* best_variant, float* times_ms);
+/* The cached batched variant for n_total points, or -1. */
+GTC_API int gtc_autotune_lookup_batched(uint32_t n_total);
 GTC_API gtc_status gtc_autotune_save(const char* path);
 GTC_API gtc_status gtc_autotune_load(const char* path);
 

@@ -69,3 +69,32 @@ def test_env_cache_file_is_loaded_on_first_use(tmp_path):
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     assert out.stdout.strip() == "3"
+
+
+def test_batched_entries_load_save_and_pin(clean, tmp_path):
+    """Batched onesweep shapes share the cache file as "batched <log2n>
+    <variant> <ms>" lines; a pinned variant overrides the tuned one, and out
+    of range variants are refused.  Host logic only (no build runs)."""
+    g = clean
+    L = g.lib()
+    nv = L.gtc_batched_num_variants()
+    assert nv >= 2 and len(g.batched_variants()) == nv
+    assert g.batched_variants()[0] == (512, 12)
+    path = tmp_path / "tune.txt"
+    path.write_text(f"batched 27 1 5.5\nbatched 27 {nv} 1.0\nbatched 40 0 1.0\n")  # the last two are ignored
+    g.autotune_load(str(path))
+    assert L.gtc_autotune_entries() == 1
+    n = 83_487_470  # ceil(log2 n) = 27
+    assert g.autotune_lookup_batched(n) == 1 and g.batched_get_variant(n) == 1
+    assert g.autotune_lookup_batched(1 << 20) == -1 and g.batched_get_variant(1 << 20) == 0
+    g.batched_set_variant(nv - 1)
+    try:
+        assert g.batched_get_variant(n) == nv - 1
+    finally:
+        g.batched_set_variant(-1)
+    assert g.batched_get_variant(n) == 1
+    with pytest.raises(g.GtcError):
+        g.batched_set_variant(nv)
+    out = str(tmp_path / "saved.txt")
+    g.autotune_save(out)
+    assert "batched 27 1 " in open(out).read()

@@ -215,3 +215,45 @@ def test_batched_rejects_bad_args(ctx):
     with pytest.raises(gtc.GtcError) as ei:
         plan.launch(pts.view(-1)[1:], offsets, n_total=64)
     assert ei.value.status == 1
+
+
+def test_every_batched_variant_identical_and_tuned(ctx, oracle):
+    """Every compiled tile shape of the segmented onesweep gives the same
+    batch, byte for byte (each cloud also against the oracle under a
+    non-default shape); the autotuner times them all on the batch and its pick
+    is what an unpinned build uses."""
+    import gtc
+    import torch
+
+    gtc.autotune_clear()
+    pts_np, offs_np = W.config4_clouds(48, seed=11)
+    pts = torch.from_numpy(pts_np).cuda()
+    offs = torch.from_numpy(offs_np.view(np.int32)).cuda()
+    n = pts_np.shape[0]
+    plan = gtc.BatchPlan(ctx, n, 48)
+    ref = None
+    try:
+        for v in range(len(gtc.batched_variants())):
+            gtc.batched_set_variant(v)
+            plan.launch(pts, offs)
+            torch.cuda.synchronize()
+            ctx.device_status()
+            got = [t.clone() for t in (plan.keys, plan.idx, plan.parent, plan.edge, plan.nodes, plan.node_offset)]
+            if ref is None:
+                ref = got
+                continue
+            for a, b in zip(ref, got):
+                assert torch.equal(a, b), v
+        for c, res in enumerate(plan.clouds()):  # the last (non-default) shape, against the oracle
+            s, e = int(offs_np[c]), int(offs_np[c + 1])
+            if c % 4 == 0:
+                _check_cloud(gtc, oracle, res, pts_np[s:e], f"variant{v}/cloud{c}")
+    finally:
+        gtc.batched_set_variant(-1)
+    r = plan.autotune(pts, offs, reps=2)
+    assert len(r["ms"]) == len(gtc.batched_variants()) and all(0 < t < 1e4 for t in r["ms"])
+    assert gtc.autotune_lookup_batched(n) == r["best"] == gtc.batched_get_variant(n)
+    plan.launch(pts, offs)
+    torch.cuda.synchronize()
+    assert torch.equal(plan.nodes, ref[4]) and torch.equal(plan.keys, ref[0])
+    gtc.autotune_clear()
