@@ -406,8 +406,9 @@ def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
     wk, wv = torch.empty_like(keys), torch.empty_like(vals)
     ka, va = torch.empty_like(keys), torch.empty_like(vals)
     sws = ctx.workspace(gtc.OP_SORT_PAIRS, n, 64)
-    # the plain sort runs the autotuner's pick for these keys
+    # both sorts run the autotuner's pick for these keys
     ctx.autotune_sort(64, n, 0, 64, keys=keys, reps=2)
+    ltune = model.autotune(keys, vals, ws=ws, keys_out=ko, vals_out=vo, reps=2)
     flags = []
 
     def learned_step():
@@ -441,7 +442,8 @@ def measure_learned(ctx, n, steps, warmup, shifted_n=8_000_000):
     out = {"learned_mkeys_s": round(n / (learned_ms * 1e-3) / 1e6, 1), "learned_ms": round(learned_ms, 4),
            "plain_mkeys_s": round(n / (plain_ms * 1e-3) / 1e6, 1), "plain_ms": round(plain_ms, 4),
            "speedup_vs_plain": round(plain_ms / learned_ms, 3), "identical": identical, "flags": fl, "n": n,
-           "buckets": B, "plain_sort_variant": gtc.autotune_lookup(64, 64, n), "train_loss": loss,
+           "buckets": B, "plain_sort_variant": gtc.autotune_lookup(64, 64, n), "learned_variant": ltune["best"],
+           "autotune_learned_ms": [round(t, 4) for t in ltune["ms"]], "train_loss": loss,
            "train_s": round(train_s, 3),
            "bucket_max_over_mean": round(float(counts.max()) / (n / B), 3),
            "shifted_n": int(shifted.numel()), "shifted_flags": int(sflags.item()), "shifted_exact": shifted_ok}

@@ -500,6 +500,13 @@ int sort_select_variant(int key_bits, int bits, uint32_t n);
 int tuned_variant(int key_bits, int bits, uint32_t n);
 // The tuned batched onesweep shape for a batch of n points, or -1 (tune.cu).
 int tuned_batched_variant(uint32_t n);
+// The tuned learned-sort grouping pass shape for n keys, or -1 (tune.cu).
+int tuned_learned_variant(uint32_t n);
+// The learned sort with the grouping passes' shape given (learned.cu).
+int learned_num_variants();
+gtc_status learned_sort_variant(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys, const uint32_t* vals,
+                                uint64_t* keys_out, uint32_t* vals_out, uint32_t n, void* ws, size_t ws_bytes,
+                                uint32_t* d_flags, gtc_stream_t stream, int variant);
 // The batched build with the segmented onesweep shape given (batched.cu).
 int batched_num_variants();
 gtc_status build_octree_batched_variant(gtc_ctx* ctx, const float* pts, const uint32_t* d_offsets,

@@ -30,6 +30,7 @@
 //               plain onesweep kernels (launched unconditionally, gated on the
 //               flag word) sort it; otherwise they return at once.
 
+#include <atomic>
 #include <cstdio>
 #include <new>
 
@@ -205,11 +206,16 @@ __global__ void __launch_bounds__(1024) adam_kernel(float* y, const float* grad,
 // onesweep pass of sort.cu with a third array).  Stable passes keep equal
 // keys in input order inside every bucket, so the in-bucket sort needs no
 // positions to order them.
-constexpr int LP_THREADS = 256;
-constexpr int LP_KPT = 16;
-constexpr int LP_TILE = LP_THREADS * LP_KPT;  // 4096 keys per pass tile
-constexpr int LP_RADIX = 128;                 // bucket-id digits of at most 7 bits
-constexpr int LP_WARPS = LP_THREADS / 32;
+// Grouping pass tile shapes (threads x keys per thread), compiled as
+// variants: pinned with gtc_learned_set_variant, else the autotuner's pick for
+// n (gtc_autotune_learned), else variant 0.
+struct LpVariant {
+  int threads, kpt;
+};
+constexpr LpVariant kLpVariants[] = {{256, 16}, {512, 12}, {384, 16}, {512, 8}};
+constexpr int kLpNumVariants = sizeof(kLpVariants) / sizeof(kLpVariants[0]);
+constexpr int LP_MIN_TILE = 4096;  // smallest tile of any variant: sizes the descriptors
+constexpr int LP_RADIX = 128;      // bucket-id digits of at most 7 bits
 
 // 0. model preparation before a sort (one thread per segment): the bucket
 // lines of model_bucket, the interior knots in Eytzinger order for the
@@ -352,38 +358,45 @@ __global__ void __launch_bounds__(1024) learned_scan_kernel(const uint32_t* tota
 // 3. one stable pass over the bucket-id digit (bid >> shift) & mask.  FIRST:
 // the caller's keys and values (values absent: the index) in, bucket ids
 // carried out; otherwise the ids are read and dropped.
+template <int THREADS, int KPT>
 struct LpSmem {
-  uint64_t keys[LP_TILE];
-  uint32_t vals[LP_TILE];
-  uint16_t bids[LP_TILE];
-  uint32_t warp_hist[LP_WARPS][LP_RADIX];
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int TILE = THREADS * KPT;
+  uint64_t keys[TILE];
+  uint32_t vals[TILE];
+  uint16_t bids[TILE];
+  uint32_t warp_hist[WARPS][LP_RADIX];
   uint32_t gbase[LP_RADIX];
   uint32_t warp_sums[LP_RADIX / 32];
   uint32_t tile_id;
 };
 
-template <bool FIRST>
-__global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
+template <bool FIRST, int THREADS, int KPT>
+__global__ void __launch_bounds__(THREADS) learned_pass_kernel(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, const uint16_t* __restrict__ bin,
     uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint16_t* __restrict__ bout, uint32_t n, int shift,
     uint32_t mask, const uint32_t* __restrict__ bin_off, uint32_t* __restrict__ desc, uint32_t* tile_counter,
     uint32_t* status, const uint32_t* flags) {
   if (*flags & (LFLAG_OVERFLOW | LFLAG_BAD_MODEL)) return;
+  using Sm = LpSmem<THREADS, KPT>;
+  constexpr int WARPS = Sm::WARPS;
+  constexpr int TILE = Sm::TILE;
+  static_assert(THREADS >= LP_RADIX, "one thread per digit");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LpSmem& s = *reinterpret_cast<LpSmem*>(smem_raw);
+  Sm& s = *reinterpret_cast<Sm*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  for (int i = tid; i < LP_WARPS * LP_RADIX; i += LP_THREADS) (&s.warp_hist[0][0])[i] = 0;
+  for (int i = tid; i < WARPS * LP_RADIX; i += THREADS) (&s.warp_hist[0][0])[i] = 0;
   if (tid == 0) s.tile_id = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const uint32_t tile = s.tile_id;
-  const uint32_t tbase = tile * LP_TILE;
+  const uint32_t tbase = tile * TILE;
 
-  uint64_t key[LP_KPT];
-  uint32_t val[LP_KPT], bd[LP_KPT];
-  const uint32_t wbase = tbase + warp * 32 * LP_KPT + lane;
+  uint64_t key[KPT];
+  uint32_t val[KPT], bd[KPT];
+  const uint32_t wbase = tbase + warp * 32 * KPT + lane;
 #pragma unroll
-  for (int j = 0; j < LP_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t pos = wbase + j * 32;
     const bool ok = pos < n;
     key[j] = ok ? kin[pos] : ~0ull;
@@ -392,7 +405,7 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
   }
   uint32_t* my_hist = s.warp_hist[warp];
 #pragma unroll
-  for (int j = 0; j < LP_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (bd[j] >> shift) & mask;
     const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
     if (__all_sync(0xffffffffu, d == d0)) {
@@ -405,7 +418,7 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
   uint32_t count = 0;
   if (tid < LP_RADIX) {
 #pragma unroll
-    for (int w = 0; w < LP_WARPS; ++w) {
+    for (int w = 0; w < WARPS; ++w) {
       const uint32_t c = s.warp_hist[w][tid];
       s.warp_hist[w][tid] = count;
       count += c;
@@ -423,11 +436,11 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
     for (int w = 0; w < LP_RADIX / 32; ++w) doff += (w < warp) ? s.warp_sums[w] : 0u;
     doff += incl - count;
 #pragma unroll
-    for (int w = 0; w < LP_WARPS; ++w) s.warp_hist[w][tid] += doff;
+    for (int w = 0; w < WARPS; ++w) s.warp_hist[w][tid] += doff;
   }
   __syncthreads();
 #pragma unroll
-  for (int j = 0; j < LP_KPT; ++j) {
+  for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (bd[j] >> shift) & mask;
     uint32_t peers = 0xffffffffu;
 #pragma unroll
@@ -454,8 +467,8 @@ __global__ void __launch_bounds__(LP_THREADS) learned_pass_kernel(
     s.gbase[tid] = bin_off[tid] + excl - doff;
   }
   __syncthreads();
-  const uint32_t valid = min((uint32_t)LP_TILE, n - tbase);
-  for (uint32_t i = tid; i < valid; i += LP_THREADS) {
+  const uint32_t valid = min((uint32_t)TILE, n - tbase);
+  for (uint32_t i = tid; i < valid; i += THREADS) {
     const uint32_t b = s.bids[i];
     const uint32_t o = s.gbase[(b >> shift) & mask] + i;
     kout[o] = s.keys[i];
@@ -768,7 +781,7 @@ struct LearnedWorkspace {
 };
 
 static size_t learned_ws_layout(uint32_t n, int B, LearnedWorkspace* W, char* p) {
-  const uint32_t ptiles = ceil_div(n > 0 ? n : 1, LP_TILE);
+  const uint32_t ptiles = ceil_div(n > 0 ? n : 1, LP_MIN_TILE);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     char* q = p ? p + o : nullptr;
@@ -849,6 +862,37 @@ gtc_status launch_count(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t
   LTRY(ctx, cudaGetLastError());
   return GTC_OK;
 }
+
+// One grouping pass with the tile shape of variant v.
+template <bool FIRST, int THREADS, int KPT>
+cudaError_t launch_lp_shape(cudaStream_t s, uint32_t n, const uint64_t* kin, const uint32_t* vin, const uint16_t* bin,
+                            uint64_t* kout, uint32_t* vout, uint16_t* bout, int shift, uint32_t mask,
+                            const uint32_t* off, uint32_t* desc, uint32_t* tc, uint32_t* status,
+                            const uint32_t* flags) {
+  using Sm = LpSmem<THREADS, KPT>;
+  cudaError_t e = kernel_setup(learned_pass_kernel<FIRST, THREADS, KPT>, THREADS, sizeof(Sm));
+  if (e != cudaSuccess) return e;
+  learned_pass_kernel<FIRST, THREADS, KPT><<<ceil_div(n, (uint32_t)Sm::TILE), THREADS, sizeof(Sm), s>>>(
+      kin, vin, bin, kout, vout, bout, n, shift, mask, off, desc, tc, status, flags);
+  return cudaGetLastError();
+}
+
+template <bool FIRST>
+cudaError_t launch_lp(int v, cudaStream_t s, uint32_t n, const uint64_t* kin, const uint32_t* vin,
+                      const uint16_t* bin, uint64_t* kout, uint32_t* vout, uint16_t* bout, int shift, uint32_t mask,
+                      const uint32_t* off, uint32_t* desc, uint32_t* tc, uint32_t* status, const uint32_t* flags) {
+#define GTC_LP(T, K) \
+  return launch_lp_shape<FIRST, T, K>(s, n, kin, vin, bin, kout, vout, bout, shift, mask, off, desc, tc, status, flags)
+  switch (v) {
+    case 1: GTC_LP(512, 12);
+    case 2: GTC_LP(384, 16);
+    case 3: GTC_LP(512, 8);
+    default: GTC_LP(256, 16);
+  }
+#undef GTC_LP
+}
+
+std::atomic<int> g_lp_pinned{-1};  // gtc_learned_set_variant
 
 gtc_status prepare_sample(gtc_ctx* ctx, gtc_learned_model* m, const uint64_t* sorted, uint32_t n, uint32_t stride,
                           cudaStream_t s) {
@@ -977,10 +1021,24 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
   return launch_count(ctx, m, keys, n, d_counts, nullptr, s);
 }
 
-GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys,
-                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
-                                        void* ws, size_t ws_bytes, uint32_t* d_flags, gtc_stream_t stream) {
+}  // extern "C"
+
+namespace gtc {
+int learned_select_variant(uint32_t n) {
+  const int pinned = g_lp_pinned.load(std::memory_order_relaxed);
+  if (pinned >= 0) return pinned;
+  const int t = tuned_learned_variant(n);
+  return (t >= 0 && t < kLpNumVariants) ? t : 0;
+}
+int learned_num_variants() { return kLpNumVariants; }
+
+// The learned sort with the grouping passes' tile shape given.
+gtc_status learned_sort_variant(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys, const uint32_t* vals,
+                                uint64_t* keys_out, uint32_t* vals_out, uint32_t n, void* ws, size_t ws_bytes,
+                                uint32_t* d_flags, gtc_stream_t stream, int variant) {
   if (!ctx || !m || !d_flags) return GTC_ERR_INVALID_ARG;
+  if (variant < 0 || variant >= kLpNumVariants)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "no such learned variant", cudaSuccess);
   if (n >= (1u << 30)) return context_error(ctx, GTC_ERR_INVALID_ARG, "n must be < 2^30", cudaSuccess);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   LTRY(ctx, cudaMemsetAsync(d_flags, 0, 4, s));
@@ -996,11 +1054,8 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
                          cudaSuccess);
   LearnedWorkspace W;
   learned_ws_layout(n, B, &W, reinterpret_cast<char*>(ws));
-  const uint32_t ptiles = ceil_div(n, LP_TILE);
   const int lb = 31 - __builtin_clz((unsigned)B);  // bucket-id bits
   const int db1 = (lb + 1) / 2, db2 = lb - db1;      // digit widths of the two passes (<= 7 each)
-  LTRY(ctx, kernel_setup(learned_pass_kernel<true>, LP_THREADS, sizeof(LpSmem)));
-  LTRY(ctx, kernel_setup(learned_pass_kernel<false>, LP_THREADS, sizeof(LpSmem)));
   LTRY(ctx, kernel_setup(bucket_sort_kernel, BS_THREADS, sizeof(BucketSmem)));
   const Launch L0 = context_launch(ctx, stream);
   LTRY(ctx, cudaMemsetAsync(W.misc, 0, 256, s));
@@ -1010,13 +1065,12 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
   if (st == GTC_OK) st = launch_count(ctx, m, keys, n, W.totals, W.bid, s);
   if (st != GTC_OK) return st;
   learned_scan_kernel<<<1, 1024, 0, s>>>(W.totals, B, db1, m->heights, W.base, W.off1, W.off2, d_flags);
-  learned_pass_kernel<true><<<ptiles, LP_THREADS, sizeof(LpSmem), s>>>(
-      keys, vals, W.bid, db2 ? W.tkeys : W.ukeys, db2 ? W.tvals : W.uvals, W.bid2, n, 0, (1u << db1) - 1, W.off1,
-      W.desc, W.misc + 1, L0.status, d_flags);
+  LTRY(ctx, cudaGetLastError());
+  LTRY(ctx, launch_lp<true>(variant, s, n, keys, vals, W.bid, db2 ? W.tkeys : W.ukeys, db2 ? W.tvals : W.uvals,
+                            W.bid2, 0, (1u << db1) - 1, W.off1, W.desc, W.misc + 1, L0.status, d_flags));
   if (db2)
-    learned_pass_kernel<false><<<ptiles, LP_THREADS, sizeof(LpSmem), s>>>(
-        W.tkeys, W.tvals, W.bid2, W.ukeys, W.uvals, nullptr, n, db1, (1u << db2) - 1, W.off2, W.desc + W.desc_words,
-        W.misc + 2, L0.status, d_flags);
+    LTRY(ctx, launch_lp<false>(variant, s, n, W.tkeys, W.tvals, W.bid2, W.ukeys, W.uvals, nullptr, db1,
+                               (1u << db2) - 1, W.off2, W.desc + W.desc_words, W.misc + 2, L0.status, d_flags));
   bucket_sort_kernel<<<B, BS_THREADS, sizeof(BucketSmem), s>>>(W.ukeys, W.uvals, W.base, W.totals, keys_out, vals_out,
                                                                W.bmin, W.bmax, d_flags);
   learned_order_check_kernel<<<ceil_div(B, 256), 256, 0, s>>>(W.totals, W.bmin, W.bmax, B, d_flags);
@@ -1036,5 +1090,32 @@ GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m
                                              nullptr, kFallbackVariant));
   return GTC_OK;
 }
+}  // namespace gtc
+
+extern "C" {
+
+GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys,
+                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
+                                        void* ws, size_t ws_bytes, uint32_t* d_flags, gtc_stream_t stream) {
+  return learned_sort_variant(ctx, m, keys, vals, keys_out, vals_out, n, ws, ws_bytes, d_flags, stream,
+                              learned_select_variant(n));
+}
+
+GTC_API int gtc_learned_num_variants(void) { return kLpNumVariants; }
+
+GTC_API gtc_status gtc_learned_variant_shape(int variant, int* threads, int* keys_per_thread) {
+  if (variant < 0 || variant >= kLpNumVariants) return GTC_ERR_INVALID_ARG;
+  if (threads) *threads = kLpVariants[variant].threads;
+  if (keys_per_thread) *keys_per_thread = kLpVariants[variant].kpt;
+  return GTC_OK;
+}
+
+GTC_API gtc_status gtc_learned_set_variant(int variant) {
+  if (variant < -1 || variant >= kLpNumVariants) return GTC_ERR_INVALID_ARG;
+  g_lp_pinned.store(variant, std::memory_order_relaxed);
+  return GTC_OK;
+}
+
+GTC_API int gtc_learned_get_variant(uint32_t n) { return learned_select_variant(n); }
 
 }  // extern "C"

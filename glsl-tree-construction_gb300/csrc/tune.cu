@@ -43,9 +43,9 @@ struct TuneEntry {
 std::mutex g_mu;
 std::map<TuneKey, TuneEntry> g_cache;
 // Other tuned shapes by (kind, ceil(log2 n)): the batched build's segmented
-// onesweep (kind "batched").
-enum TuneKind { TK_BATCHED = 0 };
-const char* const kKindName[] = {"batched"};
+// onesweep ("batched") and the learned sort's grouping passes ("learned").
+enum TuneKind { TK_BATCHED = 0, TK_LEARNED = 1 };
+const char* const kKindName[] = {"batched", "learned"};
 std::map<std::pair<int, int>, TuneEntry> g_xcache;
 bool g_env_loaded = false;
 
@@ -68,6 +68,9 @@ bool load_locked(const char* path) {
     else if (sscanf(line, "batched %d %d %f", &lg, &v, &ms) == 3 && lg >= 0 && lg <= 32 && v >= 0 &&
              v < batched_num_variants())
       g_xcache[{TK_BATCHED, lg}] = TuneEntry{v, ms};
+    else if (sscanf(line, "learned %d %d %f", &lg, &v, &ms) == 3 && lg >= 0 && lg <= 32 && v >= 0 &&
+             v < learned_num_variants())
+      g_xcache[{TK_LEARNED, lg}] = TuneEntry{v, ms};
   }
   fclose(f);
   return true;
@@ -76,7 +79,8 @@ bool load_locked(const char* path) {
 bool save_locked(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return false;
-  fprintf(f, "# gtc autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms> | batched <log2n> <variant> <ms>\n");
+  fprintf(f, "# gtc autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms>, "
+             "batched|learned <log2n> <variant> <ms>\n");
   for (const auto& kv : g_cache)
     fprintf(f, "sort %d %d %d %d %.6f\n", kv.first.key_bits, kv.first.bits, kv.first.log2n, kv.second.variant,
             kv.second.ms);
@@ -203,11 +207,56 @@ int tuned_variant(int key_bits, int bits, uint32_t n) {
   return it == g_cache.end() ? -1 : it->second.variant;
 }
 
-int tuned_batched_variant(uint32_t n) {
+static int tuned_kind_variant(int kind, uint32_t n) {
   std::lock_guard<std::mutex> g(g_mu);
   load_env_once_locked();
-  const auto it = g_xcache.find({TK_BATCHED, log2_bucket(n)});
+  const auto it = g_xcache.find({kind, log2_bucket(n)});
   return it == g_xcache.end() ? -1 : it->second.variant;
+}
+int tuned_batched_variant(uint32_t n) { return tuned_kind_variant(TK_BATCHED, n); }
+int tuned_learned_variant(uint32_t n) { return tuned_kind_variant(TK_LEARNED, n); }
+
+// Times run(variant) for every variant: `reps` timed calls after one warm-up
+// each, on a private stream, best time kept; caches the fastest for (kind,
+// ceil(log2 n)).
+template <class Run>
+static gtc_status tune_kind(gtc_ctx* ctx, int kind, int nv, uint32_t n, int reps, Run run, int* best, float* times) {
+  std::vector<float> t(nv, FLT_MAX);
+  cudaStream_t s = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  gtc_status st = GTC_OK;
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess)
+    st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
+  for (int vi = 0; vi < nv && st == GTC_OK; ++vi) {
+    for (int r = 0; r <= reps && st == GTC_OK; ++r) {  // r = 0 warms up (and sets kernel attributes)
+      cudaEventRecord(a, s);
+      st = run(vi, reinterpret_cast<gtc_stream_t>(s));
+      cudaEventRecord(b, s);
+      if (st == GTC_OK && (e = cudaEventSynchronize(b)) != cudaSuccess)
+        st = context_error(ctx, GTC_ERR_CUDA, "autotune: timed run", e);
+      float ms = 0.f;
+      if (st == GTC_OK && r > 0 && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < t[vi]) t[vi] = ms;
+    }
+  }
+  if (s) cudaStreamSynchronize(s);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (s) cudaStreamDestroy(s);
+  if (st != GTC_OK) return st;
+  int bv = 0;
+  for (int vi = 1; vi < nv; ++vi)
+    if (t[vi] < t[bv]) bv = vi;
+  if (best) *best = bv;
+  if (times)
+    for (int vi = 0; vi < nv; ++vi) times[vi] = t[vi];
+  std::lock_guard<std::mutex> g(g_mu);
+  load_env_once_locked();
+  g_xcache[{kind, log2_bucket(n)}] = TuneEntry{bv, t[bv]};
+  const char* p = getenv("GTC_TUNE_CACHE");
+  if (p && *p) save_locked(p);
+  return GTC_OK;
 }
 
 }  // namespace gtc
@@ -259,46 +308,27 @@ GTC_API gtc_status gtc_autotune_batched(gtc_ctx* ctx, const float* pts, const ui
   if (!ctx) return GTC_ERR_INVALID_ARG;
   if (n_total == 0 || reps < 1 || reps > 100)
     return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: need n_total > 0 and 1 <= reps <= 100", cudaSuccess);
-  const int nv = batched_num_variants();
-  std::vector<float> t(nv, FLT_MAX);
-  cudaStream_t s = nullptr;
-  cudaEvent_t a = nullptr, b = nullptr;
-  gtc_status st = GTC_OK;
-  cudaError_t e;
-  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess)
-    st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
-  gtc_stream_t gs = reinterpret_cast<gtc_stream_t>(s);
-  for (int vi = 0; vi < nv && st == GTC_OK; ++vi) {
-    for (int r = 0; r <= reps && st == GTC_OK; ++r) {  // r = 0 warms up (and sets kernel attributes)
-      cudaEventRecord(a, s);
-      st = build_octree_batched_variant(ctx, pts, d_offsets, n_clouds, n_total, min_coord, range, out, ws,
-                                        ws_bytes, gs, vi);
-      cudaEventRecord(b, s);
-      if (st == GTC_OK && (e = cudaEventSynchronize(b)) != cudaSuccess)
-        st = context_error(ctx, GTC_ERR_CUDA, "autotune: timed batched build", e);
-      float ms = 0.f;
-      if (st == GTC_OK && r > 0 && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < t[vi]) t[vi] = ms;
-    }
-  }
-  if (s) cudaStreamSynchronize(s);
-  if (a) cudaEventDestroy(a);
-  if (b) cudaEventDestroy(b);
-  if (s) cudaStreamDestroy(s);
-  if (st != GTC_OK) return st;
-  int bv = 0;
-  for (int vi = 1; vi < nv; ++vi)
-    if (t[vi] < t[bv]) bv = vi;
-  if (best_variant) *best_variant = bv;
-  if (times_ms)
-    for (int vi = 0; vi < nv; ++vi) times_ms[vi] = t[vi];
-  std::lock_guard<std::mutex> g(g_mu);
-  load_env_once_locked();
-  g_xcache[{TK_BATCHED, log2_bucket(n_total)}] = TuneEntry{bv, t[bv]};
-  const char* p = getenv("GTC_TUNE_CACHE");
-  if (p && *p) save_locked(p);
-  return GTC_OK;
+  auto run = [&](int v, gtc_stream_t s) {
+    return build_octree_batched_variant(ctx, pts, d_offsets, n_clouds, n_total, min_coord, range, out, ws, ws_bytes,
+                                        s, v);
+  };
+  return tune_kind(ctx, TK_BATCHED, batched_num_variants(), n_total, reps, run, best_variant, times_ms);
 }
+
+GTC_API gtc_status gtc_autotune_learned(gtc_ctx* ctx, const gtc_learned_model* model, const uint64_t* keys,
+                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
+                                        void* ws, size_t ws_bytes, uint32_t* d_flags, int reps, int* best_variant,
+                                        float* times_ms) {
+  if (!ctx) return GTC_ERR_INVALID_ARG;
+  if (n == 0 || reps < 1 || reps > 100)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: need n > 0 and 1 <= reps <= 100", cudaSuccess);
+  auto run = [&](int v, gtc_stream_t s) {
+    return learned_sort_variant(ctx, model, keys, vals, keys_out, vals_out, n, ws, ws_bytes, d_flags, s, v);
+  };
+  return tune_kind(ctx, TK_LEARNED, learned_num_variants(), n, reps, run, best_variant, times_ms);
+}
+
+GTC_API int gtc_autotune_lookup_learned(uint32_t n) { return tuned_learned_variant(n); }
 
 GTC_API int gtc_autotune_lookup_batched(uint32_t n_total) { return tuned_batched_variant(n_total); }
 

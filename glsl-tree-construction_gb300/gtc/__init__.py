@@ -630,6 +630,23 @@ class LearnedModel:
                                                             _stream()))
         return c
 
+    def autotune(self, keys, vals=None, ws=None, keys_out=None, vals_out=None, reps: int = 3) -> dict:
+        """Time every grouping-pass shape on these keys and cache the fastest
+        for n; returns {"best": variant, "ms": [per-variant best sort time]}."""
+        torch = _torch()
+        n = keys.numel()
+        keys_out = torch.empty_like(keys) if keys_out is None else keys_out
+        vals_out = torch.empty(n, dtype=torch.int32, device=keys.device) if vals_out is None else vals_out
+        ws = self.ctx.workspace(OP_LEARNED_SORT, n, 64) if ws is None else ws
+        flags = torch.zeros(1, dtype=torch.int32, device=keys.device)
+        nv = self.ctx.L.gtc_learned_num_variants()
+        times = (ctypes.c_float * nv)()
+        best = ctypes.c_int(-1)
+        self.ctx.check(self.ctx.L.gtc_autotune_learned(self.ctx.h, self.h, _ptr(keys), _ptr(vals), _ptr(keys_out),
+                                                       _ptr(vals_out), n, _ptr(ws), ws.numel(), _ptr(flags), reps,
+                                                       ctypes.byref(best), times))
+        return {"best": best.value, "ms": [float(t) for t in times]}
+
     def sort(self, keys, vals=None, ws=None, keys_out=None, vals_out=None):
         """Out-of-place learned sort; returns (keys_out, vals_out, flags tensor)."""
         torch = _torch()
@@ -641,6 +658,32 @@ class LearnedModel:
         self.ctx.check(self.ctx.L.gtc_learned_sort_u64(self.ctx.h, self.h, _ptr(keys), _ptr(vals), _ptr(keys_out),
                                                        _ptr(vals_out), n, _ptr(ws), ws.numel(), _ptr(flags), _stream()))
         return keys_out, vals_out, flags
+
+
+def learned_variants() -> list:
+    """(threads, keys per thread) of every learned grouping-pass variant."""
+    L = lib()
+    out = []
+    for v in range(L.gtc_learned_num_variants()):
+        t, k = ctypes.c_int(), ctypes.c_int()
+        if L.gtc_learned_variant_shape(v, ctypes.byref(t), ctypes.byref(k)) != 0:
+            raise GtcError(1, "gtc_learned_variant_shape")
+        out.append((t.value, k.value))
+    return out
+
+
+def learned_set_variant(v: int):
+    """Pin one grouping-pass shape for every learned sort (-1 unpins)."""
+    if lib().gtc_learned_set_variant(v) != 0:
+        raise GtcError(1, f"no learned variant {v}")
+
+
+def learned_get_variant(n: int) -> int:
+    return lib().gtc_learned_get_variant(n)
+
+
+def autotune_lookup_learned(n: int) -> int:
+    return lib().gtc_autotune_lookup_learned(n)
 
 
 def learned_buckets_for(n: int) -> int:

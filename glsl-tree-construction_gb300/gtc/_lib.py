@@ -102,6 +102,12 @@ SIGNATURES = {
     "gtc_autotune_batched": (st, [P, P, P, u32, u32, f32, f32, ctypes.POINTER(BatchBuffers), P, sz, i_,
                                   ctypes.POINTER(i_), P]),
     "gtc_autotune_lookup_batched": (i_, [u32]),
+    "gtc_learned_num_variants": (i_, []),
+    "gtc_learned_variant_shape": (st, [i_, ctypes.POINTER(i_), ctypes.POINTER(i_)]),
+    "gtc_learned_set_variant": (st, [i_]),
+    "gtc_learned_get_variant": (i_, [u32]),
+    "gtc_autotune_learned": (st, [P, P, P, P, P, P, u32, P, sz, P, i_, ctypes.POINTER(i_), P]),
+    "gtc_autotune_lookup_learned": (i_, [u32]),
     # reference-signature host shims
     "gtc_ref_compute_morton": (st, [P, P, u32, f32, f32, u32]),
     "gtc_ref_morton32_to_xyz": (None, [P, u32, f32, f32]),

@@ -413,6 +413,17 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
 GTC_API gtc_status gtc_learned_sort_u64(gtc_ctx* ctx, const gtc_learned_model* model, const uint64_t* keys,
                                         const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
                                         void* ws, size_t ws_bytes, uint32_t* d_flags, gtc_stream_t stream);
+/* Tile shapes of the learned sort's two bucket-id grouping passes compiled
+ * into the library (threads per block x keys per thread).  A sort uses the
+ * pinned variant, else the autotuner's pick for its n
+ * (gtc_autotune_learned), else variant 0.  Every variant gives identical
+ * output.  No reference counterpart. */
+GTC_API int gtc_learned_num_variants(void);
+GTC_API gtc_status gtc_learned_variant_shape(int variant, int* threads, int* keys_per_thread);
+/* Pins one variant for every learned sort; variant = -1 unpins. */
+GTC_API gtc_status gtc_learned_set_variant(int variant);
+/* The variant a learned sort of n keys uses now. */
+GTC_API int gtc_learned_get_variant(uint32_t n);
 
 /* ------------------------------------------------------ sort variants --- */
 /* Onesweep tile shapes compiled into the library (threads per block and keys
@@ -457,6 +468,16 @@ GTC_API gtc_status gtc_autotune_batched(gtc_ctx* ctx, const float* pts, const ui
                                         void* ws, size_t ws_bytes, int reps, int* best_variant, float* times_ms);
 /* The cached batched variant for n_total points, or -1. */
 GTC_API int gtc_autotune_lookup_batched(uint32_t n_total);
+/* Times every grouping-pass shape of the learned sort on the caller's keys
+ * (arguments as gtc_learned_sort_u64) and caches the fastest for
+ * ceil(log2 n).  best_variant and times_ms[gtc_learned_num_variants()] are
+ * nullable.  Synchronous. */
+GTC_API gtc_status gtc_autotune_learned(gtc_ctx* ctx, const gtc_learned_model* model, const uint64_t* keys,
+                                        const uint32_t* vals, uint64_t* keys_out, uint32_t* vals_out, uint32_t n,
+                                        void* ws, size_t ws_bytes, uint32_t* d_flags, int reps, int* best_variant,
+                                        float* times_ms);
+/* The cached learned-sort variant for n keys, or -1. */
+GTC_API int gtc_autotune_lookup_learned(uint32_t n);
 GTC_API gtc_status gtc_autotune_save(const char* path);
 GTC_API gtc_status gtc_autotune_load(const char* path);
 

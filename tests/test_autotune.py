@@ -98,3 +98,25 @@ def test_batched_entries_load_save_and_pin(clean, tmp_path):
     out = str(tmp_path / "saved.txt")
     g.autotune_save(out)
     assert "batched 27 1 " in open(out).read()
+
+
+def test_learned_entries_load_and_pin(clean, tmp_path):
+    """Learned grouping-pass shapes: "learned <log2n> <variant> <ms>" lines,
+    the pin overriding the tuned pick, range checks.  Host logic only."""
+    g = clean
+    L = g.lib()
+    nv = L.gtc_learned_num_variants()
+    assert nv >= 2 and g.learned_variants()[0] == (256, 16)
+    path = tmp_path / "tune.txt"
+    path.write_text(f"learned 26 2 3.1\nlearned 26 {nv} 1.0\n")
+    g.autotune_load(str(path))
+    assert L.gtc_autotune_entries() == 1
+    assert g.autotune_lookup_learned(1 << 26) == 2 and g.learned_get_variant(1 << 26) == 2
+    assert g.learned_get_variant(1 << 20) == 0
+    g.learned_set_variant(1)
+    try:
+        assert g.learned_get_variant(1 << 26) == 1
+    finally:
+        g.learned_set_variant(-1)
+    with pytest.raises(g.GtcError):
+        g.learned_set_variant(nv)

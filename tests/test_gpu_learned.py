@@ -186,3 +186,31 @@ def test_config5_full_64m(ctx, gtc_mod):
         ctx.device_status()
         del keys, ko, vo, k2, v2
     model.close()
+
+
+def test_every_learned_variant_identical_and_tuned(ctx, oracle, gtc_mod):
+    """Every grouping-pass shape gives byte-identical learned sorts (equal to
+    the stable onesweep); the autotuner times them all and an unpinned sort
+    then uses its pick."""
+    import torch
+
+    gtc_mod.autotune_clear()
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=4096)
+    keys = _dev(_keys(oracle, 3_000_000, seed=6))
+    n = keys.numel()
+    k2, v2 = keys.clone(), torch.arange(n, dtype=torch.int32, device="cuda")
+    ctx.sort_pairs(k2, v2, 0, 64)
+    try:
+        for v in range(len(gtc_mod.learned_variants())):
+            gtc_mod.learned_set_variant(v)
+            ko, vo, flags = model.sort(keys)
+            assert int(flags.item()) == 0, v
+            assert torch.equal(ko, k2) and torch.equal(vo, v2), v
+    finally:
+        gtc_mod.learned_set_variant(-1)
+    r = model.autotune(keys, reps=2)
+    assert len(r["ms"]) == len(gtc_mod.learned_variants()) and all(0 < t < 1e4 for t in r["ms"])
+    assert gtc_mod.autotune_lookup_learned(n) == r["best"] == gtc_mod.learned_get_variant(n)
+    ko, vo, flags = model.sort(keys)
+    assert torch.equal(ko, k2) and torch.equal(vo, v2)
+    gtc_mod.autotune_clear()
