@@ -332,7 +332,7 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     if variant is not None:
         ctx.set_sort_variant(kb, variant)
     else:  # the autotuner's pick for these keys (cached per key width, bits and ceil(log2 n))
-        ctx.autotune_sort(kb, n, 0, kb, keys=src_k, reps=3)
+        tune = ctx.autotune_sort(kb, n, 0, kb, keys=src_k, reps=3)
     ws = ctx.workspace(gtc.OP_SORT_PAIRS, n, kb)
     k, v = torch.empty_like(src_k), torch.empty_like(src_v)
     ka, va = torch.empty_like(src_k), torch.empty_like(src_v)
@@ -359,7 +359,8 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     kk = k.cpu().numpy().view(keys_np.dtype)
     vv = v.cpu().numpy().view(np.uint32)
     ok = bool(np.all(kk[1:] >= kk[:-1])) and bool(np.array_equal(keys_np[vv], kk))
-    passes = kb // 8
+    db = ctx.get_sort_digit_bits(kb, kb, n)
+    passes = (kb + db - 1) // db
     K = kb // 8
     os_ms, os_n = stages["onesweep"]
     avg = os_ms / max(os_n, 1)
@@ -370,6 +371,9 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
             "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4),
             "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
             "sort_variant": variant if variant is not None else gtc.autotune_lookup(kb, kb, n),
+            "digit_bits": ctx.get_sort_digit_bits(kb, kb, n),
+            "digit_ms": None if variant is not None else {str(d): (round(t, 4) if t else None)
+                                                          for d, t in tune["digit_ms"].items()},
             "sorted_ok": ok}, stages
 
 
@@ -649,7 +653,9 @@ def run_gtc(args):
                     "pipeline_hbm_frac": round(alg_total / (ms_per_step * 1e-3) / 1e9 / peak, 4),
                     "sort_variant": (args.sort_variant if args.sort_variant is not None
                                      else gtc.autotune_lookup(KEY_BITS, 63 - SORT_BEGIN_BIT, n)),
-                    "autotune_sort_ms": [round(t, 4) for t in tune["ms"]]},
+                    "autotune_sort_ms": [round(t, 4) for t in tune["ms"]],
+                    "autotune_digit_ms": {str(d): (round(t, 4) if t else None)
+                                          for d, t in tune.get("digit_ms", {}).items()}},
         "roofline": {"bound": "hbm", "kernel": "onesweep_kernel (one 8-bit digit pass, u64 key + u32 value)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,

@@ -240,7 +240,9 @@ gtc_status sort_pairs_impl(gtc_ctx* ctx, K* keys, uint32_t* vals, K* keys_alt, u
   if (n == 0) return GTC_OK;
   GTC_ARG(ctx, keys && keys_alt, "keys and keys_alt are required");
   GTC_ARG(ctx, !vals || vals_alt, "vals_alt is required with vals");
-  const int passes = passes_for(begin_bit, end_bit);
+  // digit width: pinned, else the autotuner's pick, else 8 bits
+  const int db = sort_select_digit_bits(W, end_bit - begin_bit, n);
+  const int passes = (end_bit - begin_bit + db - 1) / db;
   gtc_status st = resolve_ws(ctx, ws, ws_bytes, sort_workspace_bytes(n, passes, 0));
   if (st != GTC_OK) return st;
   const Launch L = launch_of(ctx, stream);
@@ -258,7 +260,7 @@ gtc_status sort_pairs_impl(gtc_ctx* ctx, K* keys, uint32_t* vals, K* keys_alt, u
   }
   {
     StageTimer t(ctx, stream, GTC_STAGE_HISTOGRAM);
-    GTC_TRY(ctx, launch_global_hist<K>(L, keys, n, begin_bit, end_bit, Wk, passes));
+    GTC_TRY(ctx, launch_global_hist<K>(L, keys, n, begin_bit, end_bit, Wk, passes, db));
   }
   bool in_alt = false;
   {
@@ -266,7 +268,7 @@ gtc_status sort_pairs_impl(gtc_ctx* ctx, K* keys, uint32_t* vals, K* keys_alt, u
     if (ctx->profiling)
       for (int i = 0; i < 2 * passes; ++i) ev.push_back(get_event(ctx));
     GTC_TRY(ctx, launch_onesweep_passes<K>(L, keys, vals, keys_alt, vals_alt, n, begin_bit, end_bit, Wk, passes,
-                                           &in_alt, ev.empty() ? nullptr : ev.data()));
+                                           &in_alt, ev.empty() ? nullptr : ev.data(), -1, false, db));
     for (int p = 0; p < (int)ev.size() / 2; ++p) ctx->pending.push_back({ev[2 * p], ev[2 * p + 1], GTC_STAGE_ONESWEEP});
   }
   if (in_alt) {
@@ -630,7 +632,9 @@ GTC_API gtc_status gtc_workspace_size(gtc_ctx* ctx, gtc_op op, uint32_t n, int k
   if (key_bits != 32 && key_bits != 64) return fail(ctx, GTC_ERR_INVALID_ARG, "key_bits must be 32 or 64");
   const int passes = key_bits / 8;
   switch (op) {
-    case GTC_OP_SORT_PAIRS:
+    case GTC_OP_SORT_PAIRS:  // room for the passes of the narrowest digit width the sort may use
+      *bytes = sort_workspace_bytes(n, std::min(sort_max_passes(), (key_bits + 5) / 6), 0);
+      return GTC_OK;
     case GTC_OP_GLOBAL_HISTOGRAM: *bytes = sort_workspace_bytes(n, passes, 0); return GTC_OK;
     case GTC_OP_UNIQUE:
     case GTC_OP_PARTIAL_SUM: *bytes = scan_workspace_bytes(n); return GTC_OK;

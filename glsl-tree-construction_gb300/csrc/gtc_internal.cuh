@@ -484,20 +484,30 @@ cudaError_t launch_run_fixup(const Launch& L, K* keys, uint32_t* vals, K* scratc
 
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
-                               const SortWorkspace& W, int passes);
+                               const SortWorkspace& W, int passes, int db = 8);
 // variant < 0: the pinned variant, else the autotuned one for (key width,
 // bits, n), else the built-in default.  iota_vals: the values' input is the
 // position (vals is still the buffer the payload lives in between passes),
-// made by the first pass instead of read.
+// made by the first pass instead of read.  db: digit width in bits (1..8);
+// pass p sorts bits [begin_bit + db p, begin_bit + db (p + 1)), and the
+// histogram must have been built with the same width.
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
                                    bool* result_in_alt, cudaEvent_t* ev_pass /* nullable [2*passes] */,
-                                   int variant = -1, bool iota_vals = false);
+                                   int variant = -1, bool iota_vals = false, int db = 8);
 // The variant a sort of n keys of key_bits width over `bits` bits will use.
 int sort_select_variant(int key_bits, int bits, uint32_t n);
 // Autotuner cache (tune.cu): the tuned variant for (key width, bits, n), or -1.
 int tuned_variant(int key_bits, int bits, uint32_t n);
+// The tuned digit width (6..8) for (key width, bits, n), or -1 (tune.cu).
+int tuned_digit_bits(int key_bits, int bits, uint32_t n);
+// Digit width of a sort (sort.cu): pinned, else tuned, else 8; and whether a
+// width fits the bit range in the workspace's passes.
+int sort_select_digit_bits(int key_bits, int bits, uint32_t n);
+bool sort_digit_bits_ok(int bits, int db);
+bool sort_set_digit_bits(int key_bits, int db);
+int sort_max_passes();
 // The tuned batched onesweep shape for a batch of n points, or -1 (tune.cu).
 int tuned_batched_variant(uint32_t n);
 // The tuned learned-sort grouping pass shape for n keys, or -1 (tune.cu).

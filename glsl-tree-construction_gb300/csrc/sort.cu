@@ -54,12 +54,13 @@ __device__ __forceinline__ uint32_t scan256_exclusive(uint32_t v, uint32_t* warp
 
 // ------------------------------------------------------ global histogram ---
 template <class K>
-__device__ __forceinline__ void hist_add(uint32_t (*s_hist)[RADIX], K k, int begin_bit, int end_bit, int passes) {
+__device__ __forceinline__ void hist_add(uint32_t (*s_hist)[RADIX], K k, int begin_bit, int end_bit, int passes,
+                                         int db) {
 #pragma unroll
   for (int p = 0; p < MAX_PASSES; ++p) {
     if (p < passes) {
-      const int sh = begin_bit + 8 * p;
-      const int bits = min(8, end_bit - sh);
+      const int sh = begin_bit + db * p;
+      const int bits = min(db, end_bit - sh);
       const uint32_t d = (uint32_t)(k >> sh) & ((1u << bits) - 1u);
       atomicAdd(&s_hist[p][d], 1u);
     }
@@ -127,7 +128,7 @@ __device__ __forceinline__ void zero_region(uint32_t* p, size_t words) {
 
 template <class K, int THREADS>
 __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restrict__ keys, uint32_t n, int begin_bit,
-                                                              int end_bit, int passes, uint32_t* counts,
+                                                              int end_bit, int passes, int db, uint32_t* counts,
                                                               uint32_t* bin_offsets, uint32_t* done,
                                                               uint32_t* zero_ptr, size_t zero_words,
                                                               const uint32_t* run_if) {
@@ -145,10 +146,10 @@ __global__ void __launch_bounds__(THREADS) global_hist_kernel(const K* __restric
     const uint4 q = __ldcs(reinterpret_cast<const uint4*>(keys) + v);
     const K* kk = reinterpret_cast<const K*>(&q);
 #pragma unroll
-    for (int e = 0; e < VEC; ++e) hist_add<K>(s_hist, kk[e], begin_bit, end_bit, passes);
+    for (int e = 0; e < VEC; ++e) hist_add<K>(s_hist, kk[e], begin_bit, end_bit, passes, db);
   }
   for (size_t i = (size_t)nvec * VEC + (size_t)blockIdx.x * THREADS + threadIdx.x; i < n; i += stride)
-    hist_add<K>(s_hist, keys[i], begin_bit, end_bit, passes);
+    hist_add<K>(s_hist, keys[i], begin_bit, end_bit, passes, db);
   hist_finish<THREADS>(s_hist, passes, counts, bin_offsets, done, &s_last);
 }
 
@@ -1050,18 +1051,19 @@ SortWorkspace carve_sort_workspace(void* ws, uint32_t n, int passes, int /*tile_
 
 template <class K>
 cudaError_t launch_global_hist(const Launch& L, const K* keys, uint32_t n, int begin_bit, int end_bit,
-                               const SortWorkspace& W, int passes) {
+                               const SortWorkspace& W, int passes, int db) {
+  if (db < 1 || db > 8 || passes < 1 || passes > MAX_PASSES) return cudaErrorInvalidValue;
   constexpr int T = 512;
   const uint32_t want = ceil_div(n, T * 16);
   const uint32_t grid = max(1u, min(want, (uint32_t)L.num_sms * 2));
-  global_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(keys, n, begin_bit, end_bit, passes, W.counts, W.bin_offsets,
-                                                     W.header, W.desc, W.desc_words, L.run_if);
+  global_hist_kernel<K, T><<<grid, T, 0, L.stream>>>(keys, n, begin_bit, end_bit, passes, db, W.counts,
+                                                     W.bin_offsets, W.header, W.desc, W.desc_words, L.run_if);
   return cudaGetLastError();
 }
 template cudaError_t launch_global_hist<uint32_t>(const Launch&, const uint32_t*, uint32_t, int, int,
-                                                  const SortWorkspace&, int);
+                                                  const SortWorkspace&, int, int);
 template cudaError_t launch_global_hist<uint64_t>(const Launch&, const uint64_t*, uint32_t, int, int,
-                                                  const SortWorkspace&, int);
+                                                  const SortWorkspace&, int, int);
 
 template <class K>
 cudaError_t launch_morton_hist(const Launch& L, const float4* pts, K* keys, uint32_t n, float mn, float rg,
@@ -1095,7 +1097,8 @@ template cudaError_t launch_morton_hist<uint64_t>(const Launch&, const float4*, 
 template <class K>
 cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt,
                                    uint32_t n, int begin_bit, int end_bit, const SortWorkspace& W, int passes,
-                                   bool* result_in_alt, cudaEvent_t* ev, int variant, bool iota_vals) {
+                                   bool* result_in_alt, cudaEvent_t* ev, int variant, bool iota_vals, int db) {
+  if (db < 1 || db > 8 || passes < 1 || passes > MAX_PASSES) return cudaErrorInvalidValue;
   const int v = (variant >= 0 && variant < kNumVariants) ? variant
                                                           : sort_select_variant(8 * sizeof(K), end_bit - begin_bit, n);
   const bool hv = vals != nullptr;
@@ -1104,8 +1107,8 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
   uint32_t* src_v = (hv && iota_vals) ? nullptr : vals;  // the first pass makes the iota payload itself
   uint32_t* dst_v = vals_alt;
   for (int p = 0; p < passes; ++p) {
-    const int shift = begin_bit + 8 * p;
-    const int bits = min(8, end_bit - shift);
+    const int shift = begin_bit + db * p;
+    const int bits = min(db, end_bit - shift);
     const uint32_t dmask = (1u << bits) - 1u;
     if (ev) cudaEventRecord(ev[2 * p], L.stream);
     cudaError_t e = launch_variant<K>(v, hv, L, src_k, src_v, dst_k, dst_v, n, shift, dmask, W.bin_offsets + p * RADIX,
@@ -1124,10 +1127,32 @@ cudaError_t launch_onesweep_passes(const Launch& L, K* keys, uint32_t* vals, K* 
 }
 template cudaError_t launch_onesweep_passes<uint32_t>(const Launch&, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*, int, bool);
+                                                      cudaEvent_t*, int, bool, int);
 template cudaError_t launch_onesweep_passes<uint64_t>(const Launch&, uint64_t*, uint32_t*, uint64_t*, uint32_t*,
                                                       uint32_t, int, int, const SortWorkspace&, int, bool*,
-                                                      cudaEvent_t*, int, bool);
+                                                      cudaEvent_t*, int, bool, int);
+
+// Digit width of a sort: 8 bits, or 7 or 6 where the bit range still fits
+// in MAX_PASSES passes.  Pinned per key width (gtc_sort_set_digit_bits), else
+// the autotuner's pick for (key width, bits, n), else 8.
+static std::atomic<int> g_pinned_db[2] = {{-1}, {-1}};
+
+bool sort_digit_bits_ok(int bits, int db) { return db >= 6 && db <= 8 && (bits + db - 1) / db <= MAX_PASSES; }
+
+int sort_select_digit_bits(int key_bits, int bits, uint32_t n) {
+  const int pinned = g_pinned_db[key_bits == 64].load(std::memory_order_relaxed);
+  if (pinned > 0 && sort_digit_bits_ok(bits, pinned)) return pinned;
+  const int t = tuned_digit_bits(key_bits, bits, n);
+  return (t > 0 && sort_digit_bits_ok(bits, t)) ? t : 8;
+}
+
+bool sort_set_digit_bits(int key_bits, int db) {
+  if (db != -1 && (db < 6 || db > 8)) return false;
+  g_pinned_db[key_bits == 64].store(db, std::memory_order_relaxed);
+  return true;
+}
+
+int sort_max_passes() { return MAX_PASSES; }
 
 int sort_num_variants() { return kNumVariants; }
 int sort_get_variant(int key_bits) {

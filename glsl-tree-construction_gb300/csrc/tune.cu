@@ -38,6 +38,7 @@ struct TuneKey {
 struct TuneEntry {
   int variant;
   float ms;
+  int db = 8;  // sort entries: digit width in bits
 };
 
 std::mutex g_mu;
@@ -60,11 +61,12 @@ bool load_locked(const char* path) {
   if (!f) return false;
   char line[256];
   while (fgets(line, sizeof line, f)) {
-    int kb, bits, lg, v;
+    int kb, bits, lg, v, db = 8;
     float ms;
-    if (sscanf(line, "sort %d %d %d %d %f", &kb, &bits, &lg, &v, &ms) == 5 && (kb == 32 || kb == 64) &&
-        bits >= 1 && bits <= kb && lg >= 0 && lg <= 32 && v >= 0 && v < sort_num_variants())
-      g_cache[TuneKey{kb, bits, lg}] = TuneEntry{v, ms};
+    const int got = sscanf(line, "sort %d %d %d %d %f %d", &kb, &bits, &lg, &v, &ms, &db);
+    if (got >= 5 && (kb == 32 || kb == 64) && bits >= 1 && bits <= kb && lg >= 0 && lg <= 32 && v >= 0 &&
+        v < sort_num_variants() && sort_digit_bits_ok(bits, db))
+      g_cache[TuneKey{kb, bits, lg}] = TuneEntry{v, ms, db};
     else if (sscanf(line, "batched %d %d %f", &lg, &v, &ms) == 3 && lg >= 0 && lg <= 32 && v >= 0 &&
              v < batched_num_variants())
       g_xcache[{TK_BATCHED, lg}] = TuneEntry{v, ms};
@@ -79,11 +81,11 @@ bool load_locked(const char* path) {
 bool save_locked(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return false;
-  fprintf(f, "# gtc autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms>, "
+  fprintf(f, "# gtc autotune cache: sort <key_bits> <bits> <log2n> <variant> <ms> <digit bits>, "
              "batched|learned <log2n> <variant> <ms>\n");
   for (const auto& kv : g_cache)
-    fprintf(f, "sort %d %d %d %d %.6f\n", kv.first.key_bits, kv.first.bits, kv.first.log2n, kv.second.variant,
-            kv.second.ms);
+    fprintf(f, "sort %d %d %d %d %.6f %d\n", kv.first.key_bits, kv.first.bits, kv.first.log2n, kv.second.variant,
+            kv.second.ms, kv.second.db);
   for (const auto& kv : g_xcache)
     fprintf(f, "%s %d %d %.6f\n", kKindName[kv.first.first], kv.first.second, kv.second.variant, kv.second.ms);
   fclose(f);
@@ -114,10 +116,14 @@ __global__ void tune_fill_kernel(K* keys, uint32_t* vals, uint32_t n, uint64_t s
   }
 }
 
+// Times every variant at 8-bit digits, then the fastest variant at 7- and
+// 6-bit digits (where the bit range fits the workspace's passes), and caches
+// the fastest (variant, digit width).  digit_ms[0..2]: 6, 7, 8 bits (FLT_MAX
+// where a width does not fit).
 template <class K>
 gtc_status tune_impl(gtc_ctx* ctx, int begin_bit, int end_bit, uint32_t n, const void* sample, int reps, int* best,
-                     float* times_ms) {
-  const int passes = (end_bit - begin_bit + 7) / 8;
+                     float* times_ms, int* best_db, float* digit_ms) {
+  const int passes = sort_max_passes();  // workspace room for any digit width
   const int nv = sort_num_variants();
   std::vector<void*> bufs;
   cudaStream_t s = nullptr;
@@ -130,8 +136,10 @@ gtc_status tune_impl(gtc_ctx* ctx, int begin_bit, int end_bit, uint32_t n, const
     return p;
   };
   std::vector<float> t(nv, FLT_MAX);
+  float dt[3] = {FLT_MAX, FLT_MAX, FLT_MAX};  // 6, 7, 8-bit digits at the best variant
+  int bv = 0;
+  cudaError_t e = cudaSuccess;
   do {
-    cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess) {
       st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
@@ -156,27 +164,37 @@ gtc_status tune_impl(gtc_ctx* ctx, int begin_bit, int end_bit, uint32_t n, const
     }
     const Launch L = context_launch(ctx, s);
     const SortWorkspace W = carve_sort_workspace(ws, n, passes, 0);
-    for (int vi = 0; vi < nv && st == GTC_OK; ++vi) {
+    // best time of `reps` sorts (after one warm-up) of variant vi at db-bit digits
+    auto time_sort = [&](int vi, int db, float* out) {
+      const int np = (end_bit - begin_bit + db - 1) / db;
       for (int r = 0; r <= reps; ++r) {  // r = 0 warms up (and sets kernel attributes)
         bool in_alt = false;
         cudaMemcpyAsync(k, src_k, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(v, src_v, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
         cudaEventRecord(a, s);
         cudaMemsetAsync(W.header, 0, W.header_words * 4, s);
-        e = launch_global_hist<K>(L, k, n, begin_bit, end_bit, W, passes);
+        e = launch_global_hist<K>(L, k, n, begin_bit, end_bit, W, np, db);
         if (e == cudaSuccess)
-          e = launch_onesweep_passes<K>(L, k, v, ka, va, n, begin_bit, end_bit, W, passes, &in_alt, nullptr, vi);
+          e = launch_onesweep_passes<K>(L, k, v, ka, va, n, begin_bit, end_bit, W, np, &in_alt, nullptr, vi, false,
+                                        db);
         cudaEventRecord(b, s);
         if (e == cudaSuccess) e = cudaEventSynchronize(b);
         if (e != cudaSuccess) {
           st = context_error(ctx, GTC_ERR_CUDA, "autotune: timed sort", e);
-          break;
+          return;
         }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, a, b);
-        if (r > 0 && ms < t[vi]) t[vi] = ms;
+        if (r > 0 && ms < *out) *out = ms;
       }
-    }
+    };
+    for (int vi = 0; vi < nv && st == GTC_OK; ++vi) time_sort(vi, 8, &t[vi]);
+    if (st != GTC_OK) break;
+    for (int vi = 1; vi < nv; ++vi)
+      if (t[vi] < t[bv]) bv = vi;
+    dt[2] = t[bv];
+    for (int db = 7; db >= 6 && st == GTC_OK; --db)
+      if (sort_digit_bits_ok(end_bit - begin_bit, db)) time_sort(bv, db, &dt[db - 6]);
   } while (false);
   if (s) cudaStreamSynchronize(s);
   for (void* p : bufs) cudaFree(p);
@@ -184,15 +202,18 @@ gtc_status tune_impl(gtc_ctx* ctx, int begin_bit, int end_bit, uint32_t n, const
   if (b) cudaEventDestroy(b);
   if (s) cudaStreamDestroy(s);
   if (st != GTC_OK) return st;
-  int bv = 0;
-  for (int vi = 1; vi < nv; ++vi)
-    if (t[vi] < t[bv]) bv = vi;
+  int bdb = 8;
+  for (int db = 6; db <= 7; ++db)
+    if (dt[db - 6] < dt[bdb - 6]) bdb = db;
   if (best) *best = bv;
   if (times_ms)
     for (int vi = 0; vi < nv; ++vi) times_ms[vi] = t[vi];
+  if (best_db) *best_db = bdb;
+  if (digit_ms)
+    for (int i = 0; i < 3; ++i) digit_ms[i] = dt[i];
   std::lock_guard<std::mutex> g(g_mu);
   load_env_once_locked();
-  g_cache[TuneKey{(int)(8 * sizeof(K)), end_bit - begin_bit, log2_bucket(n)}] = TuneEntry{bv, t[bv]};
+  g_cache[TuneKey{(int)(8 * sizeof(K)), end_bit - begin_bit, log2_bucket(n)}] = TuneEntry{bv, dt[bdb - 6], bdb};
   const char* p = getenv("GTC_TUNE_CACHE");
   if (p && *p) save_locked(p);
   return GTC_OK;
@@ -205,6 +226,13 @@ int tuned_variant(int key_bits, int bits, uint32_t n) {
   load_env_once_locked();
   const auto it = g_cache.find(TuneKey{key_bits, bits, log2_bucket(n)});
   return it == g_cache.end() ? -1 : it->second.variant;
+}
+
+int tuned_digit_bits(int key_bits, int bits, uint32_t n) {
+  std::lock_guard<std::mutex> g(g_mu);
+  load_env_once_locked();
+  const auto it = g_cache.find(TuneKey{key_bits, bits, log2_bucket(n)});
+  return it == g_cache.end() ? -1 : it->second.db;
 }
 
 static int tuned_kind_variant(int kind, uint32_t n) {
@@ -272,8 +300,38 @@ GTC_API gtc_status gtc_autotune_sort(gtc_ctx* ctx, int key_bits, int begin_bit, 
     return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: bad key width or bit range", cudaSuccess);
   if (n == 0 || n >= (1u << 30) || reps < 1 || reps > 100)
     return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: need 0 < n < 2^30 and 1 <= reps <= 100", cudaSuccess);
-  return key_bits == 32 ? tune_impl<uint32_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms)
-                        : tune_impl<uint64_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms);
+  return key_bits == 32 ? tune_impl<uint32_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms,
+                                              nullptr, nullptr)
+                        : tune_impl<uint64_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms,
+                                              nullptr, nullptr);
+}
+
+GTC_API gtc_status gtc_autotune_sort_ex(gtc_ctx* ctx, int key_bits, int begin_bit, int end_bit, uint32_t n,
+                                        const void* d_sample_keys, int reps, int* best_variant, float* times_ms,
+                                        int* best_digit_bits, float* digit_times_ms) {
+  if (!ctx) return GTC_ERR_INVALID_ARG;
+  if ((key_bits != 32 && key_bits != 64) || begin_bit < 0 || begin_bit >= end_bit || end_bit > key_bits)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: bad key width or bit range", cudaSuccess);
+  if (n == 0 || n >= (1u << 30) || reps < 1 || reps > 100)
+    return context_error(ctx, GTC_ERR_INVALID_ARG, "autotune: need 0 < n < 2^30 and 1 <= reps <= 100", cudaSuccess);
+  return key_bits == 32 ? tune_impl<uint32_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms,
+                                              best_digit_bits, digit_times_ms)
+                        : tune_impl<uint64_t>(ctx, begin_bit, end_bit, n, d_sample_keys, reps, best_variant, times_ms,
+                                              best_digit_bits, digit_times_ms);
+}
+
+GTC_API int gtc_autotune_lookup_digit_bits(int key_bits, int bits, uint32_t n) {
+  return tuned_digit_bits(key_bits, bits, n);
+}
+
+GTC_API gtc_status gtc_sort_set_digit_bits(int key_bits, int digit_bits) {
+  if (key_bits != 32 && key_bits != 64) return GTC_ERR_INVALID_ARG;
+  return sort_set_digit_bits(key_bits, digit_bits) ? GTC_OK : GTC_ERR_INVALID_ARG;
+}
+
+GTC_API int gtc_sort_get_digit_bits(int key_bits, int bits, uint32_t n) {
+  if ((key_bits != 32 && key_bits != 64) || bits < 1 || bits > key_bits) return -1;
+  return sort_select_digit_bits(key_bits, bits, n);
 }
 
 GTC_API int gtc_autotune_lookup(int key_bits, int bits, uint32_t n) { return tuned_variant(key_bits, bits, n); }

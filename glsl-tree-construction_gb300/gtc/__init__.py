@@ -236,6 +236,13 @@ class Context:
             out.append((t.value, k.value))
         return out
 
+    def set_sort_digit_bits(self, key_bits: int, db: int):
+        """Pin the sort's digit width (6..8 bits; -1 unpins)."""
+        self.check(self.L.gtc_sort_set_digit_bits(key_bits, db))
+
+    def get_sort_digit_bits(self, key_bits: int, bits: int, n: int) -> int:
+        return self.L.gtc_sort_get_digit_bits(key_bits, bits, n)
+
     def set_sort_variant(self, key_bits: int, v: int):
         self.check(self.L.gtc_sort_set_variant(key_bits, v))
 
@@ -250,15 +257,23 @@ class Context:
         end_bit = key_bits if end_bit is None else end_bit
         nv = self.L.gtc_sort_num_variants()
         times = (ctypes.c_float * nv)()
+        dtimes = (ctypes.c_float * 3)()
         best = ctypes.c_int(-1)
-        self.check(self.L.gtc_autotune_sort(self.h, key_bits, begin_bit, end_bit, n, _ptr(keys), reps,
-                                            ctypes.byref(best), times))
-        return {"best": best.value, "ms": [float(t) for t in times]}
+        bdb = ctypes.c_int(-1)
+        self.check(self.L.gtc_autotune_sort_ex(self.h, key_bits, begin_bit, end_bit, n, _ptr(keys), reps,
+                                               ctypes.byref(best), times, ctypes.byref(bdb), dtimes))
+        big = 3.0e38  # widths that do not fit the bit range report FLT_MAX
+        return {"best": best.value, "ms": [float(t) for t in times], "digit_bits": bdb.value,
+                "digit_ms": {6 + i: (float(dtimes[i]) if dtimes[i] < big else None) for i in range(3)}}
 
 
 def autotune_lookup(key_bits: int, bits: int, n: int) -> int:
     """The autotuned onesweep variant for a sort of that shape, or -1."""
     return int(lib().gtc_autotune_lookup(key_bits, bits, n))
+
+
+def autotune_lookup_digit_bits(key_bits: int, bits: int, n: int) -> int:
+    return lib().gtc_autotune_lookup_digit_bits(key_bits, bits, n)
 
 
 def autotune_save(path: str):

@@ -90,6 +90,10 @@ SIGNATURES = {
     "gtc_export_le": (st, [ctypes.c_char_p, P, sz, i_, i_]),
     "gtc_autotune_sort": (st, [P, i_, i_, i_, u32, P, i_, ctypes.POINTER(i_), P]),
     "gtc_autotune_lookup": (i_, [i_, i_, u32]),
+    "gtc_autotune_sort_ex": (st, [P, i_, i_, i_, u32, P, i_, ctypes.POINTER(i_), P, ctypes.POINTER(i_), P]),
+    "gtc_autotune_lookup_digit_bits": (i_, [i_, i_, u32]),
+    "gtc_sort_set_digit_bits": (st, [i_, i_]),
+    "gtc_sort_get_digit_bits": (i_, [i_, i_, u32]),
     "gtc_autotune_record": (st, [i_, i_, u32, i_, f32]),
     "gtc_autotune_clear": (st, []),
     "gtc_autotune_entries": (i_, []),

@@ -435,6 +435,16 @@ GTC_API gtc_status gtc_sort_variant_shape(int variant, int* threads, int* keys_p
  * choice); variant = -1 unpins. */
 GTC_API gtc_status gtc_sort_set_variant(int key_bits, int variant);
 GTC_API int gtc_sort_get_variant(int key_bits);
+/* Digit width of gtc_sort_pairs_u32/u64: 8 bits (4 / 8 passes over full
+ * keys), or 7 or 6 where the bit range fits in 8 passes.  Pins one width
+ * for every sort of that key width (6..8; -1 unpins: the autotuner's pick,
+ * else 8); a pinned width that does not fit a sort's range is ignored for it.
+ * gtc_sort_get_digit_bits returns the width a sort of `bits` bits over n keys
+ * uses.  The reference's radix is fixed at 8 bits (new_radix_sort.comp:28-33);
+ * the sort's output does not depend on the width.  gtc_workspace_size
+ * (GTC_OP_SORT_PAIRS) leaves room for the passes of the narrowest width. */
+GTC_API gtc_status gtc_sort_set_digit_bits(int key_bits, int digit_bits);
+GTC_API int gtc_sort_get_digit_bits(int key_bits, int bits, uint32_t n);
 
 /* Radix tree method, process-wide: 1 (default) builds each node from its
  * split with nearest-smaller queries over a shared-memory window of
@@ -453,8 +463,19 @@ GTC_API int gtc_tree_get_method(void);
  * loaded on first use and rewritten after each tuning. */
 GTC_API gtc_status gtc_autotune_sort(gtc_ctx* ctx, int key_bits, int begin_bit, int end_bit, uint32_t n,
                                      const void* d_sample_keys, int reps, int* best_variant, float* times_ms);
+/* gtc_autotune_sort with the second axis reported: after the variants (at
+ * 8-bit digits), the fastest variant is timed at 7- and 6-bit digits where
+ * the bit range fits in 8 passes (32-bit keys, and 64-bit sorts of at most
+ * 48 bits), and the fastest digit width is cached with the variant.
+ * best_digit_bits and digit_times_ms[3] (6, 7, 8 bits; FLT_MAX where a width
+ * does not fit) are nullable. */
+GTC_API gtc_status gtc_autotune_sort_ex(gtc_ctx* ctx, int key_bits, int begin_bit, int end_bit, uint32_t n,
+                                        const void* d_sample_keys, int reps, int* best_variant, float* times_ms,
+                                        int* best_digit_bits, float* digit_times_ms);
 /* The cached variant for a sort of that shape, or -1. */
 GTC_API int gtc_autotune_lookup(int key_bits, int bits, uint32_t n);
+/* The cached digit width for a sort of that shape, or -1. */
+GTC_API int gtc_autotune_lookup_digit_bits(int key_bits, int bits, uint32_t n);
 GTC_API gtc_status gtc_autotune_record(int key_bits, int bits, uint32_t n, int variant, float ms);
 GTC_API gtc_status gtc_autotune_clear(void);
 GTC_API int gtc_autotune_entries(void);

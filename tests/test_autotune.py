@@ -120,3 +120,31 @@ def test_learned_entries_load_and_pin(clean, tmp_path):
         g.learned_set_variant(-1)
     with pytest.raises(g.GtcError):
         g.learned_set_variant(nv)
+
+
+def test_sort_entries_carry_the_digit_width(clean, tmp_path):
+    """Sort entries carry the tuned digit width as a sixth field (absent: 8
+    bits).  A width whose passes do not fit the bit range (6-bit digits over
+    64 bits would need 11 passes) is refused on load; a pinned width overrides
+    the tuned one only where it fits."""
+    g = clean
+    L = g.lib()
+    path = tmp_path / "tune.txt"
+    path.write_text("sort 32 32 24 16 0.43 7\nsort 64 40 24 0 0.40\nsort 64 64 24 2 1.0 6\n")
+    g.autotune_load(str(path))
+    assert L.gtc_autotune_entries() == 2
+    assert g.autotune_lookup_digit_bits(32, 32, 1 << 24) == 7 and g.autotune_lookup(32, 32, 1 << 24) == 16
+    assert g.autotune_lookup_digit_bits(64, 40, 1 << 24) == 8
+    assert g.autotune_lookup_digit_bits(64, 64, 1 << 24) == -1
+    assert L.gtc_sort_get_digit_bits(32, 32, 1 << 24) == 7
+    assert L.gtc_sort_get_digit_bits(64, 64, 1 << 24) == 8
+    assert L.gtc_sort_set_digit_bits(64, 6) == 0
+    try:
+        assert L.gtc_sort_get_digit_bits(64, 40, 1 << 24) == 6   # 7 passes: fits
+        assert L.gtc_sort_get_digit_bits(64, 64, 1 << 24) == 8   # 11 passes: does not
+    finally:
+        L.gtc_sort_set_digit_bits(64, -1)
+    assert L.gtc_sort_set_digit_bits(32, 5) != 0 and L.gtc_sort_set_digit_bits(32, 9) != 0
+    out = str(tmp_path / "saved.txt")
+    g.autotune_save(out)
+    assert "sort 32 32 24 16 0.430000 7" in open(out).read()
