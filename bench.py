@@ -218,7 +218,8 @@ def cpu_threads():
 def octree_config(n):
     """The workload's config object, the same in both arms (this project's
     build and the reference arm), so that the two lines name one workload."""
-    return {"workload": WORKLOAD, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
+    name = WORKLOAD if n == N_POINTS else f"octree_clustered_{n}_u64"
+    return {"workload": name, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
             "payload": "u32 point index",
             "cloud": "32-component Gaussian mixture (sigma 0.5% of the domain) + 2% uniform noise, seed = rank"}
 
