@@ -140,6 +140,12 @@ gtc_status tune_impl(gtc_ctx* ctx, int begin_bit, int end_bit, uint32_t n, const
   int bv = 0;
   cudaError_t e = cudaSuccess;
   do {
+    // The sample is copied on a private stream: first let every queued write
+    // of the caller's keys finish.
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) {
+      st = context_error(ctx, GTC_ERR_CUDA, "autotune: sync", e);
+      break;
+    }
     if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess) {
       st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
@@ -254,6 +260,9 @@ static gtc_status tune_kind(gtc_ctx* ctx, int kind, int nv, uint32_t n, int reps
   cudaEvent_t a = nullptr, b = nullptr;
   gtc_status st = GTC_OK;
   cudaError_t e;
+  // The runs go to a private stream: first let every queued write of the
+  // caller's inputs finish.
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return context_error(ctx, GTC_ERR_CUDA, "autotune: sync", e);
   if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&a)) != cudaSuccess || (e = cudaEventCreate(&b)) != cudaSuccess)
     st = context_error(ctx, GTC_ERR_CUDA, "autotune: stream/event creation", e);
