@@ -58,8 +58,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="octree workload: skip the sort / learned / batched forms measured after the build")
-    ap.add_argument("--workload", choices=["octree", "sort", "learned", "batched", "cub_sort"], default="octree",
+    ap.add_argument("--workload", choices=["octree", "sort", "sort_sweep", "learned", "batched", "cub_sort"],
+                    default="octree",
                     help="octree: the 10M clustered full build (default); sort: onesweep pairs sort only; "
+                         "sort_sweep: the sort at n = 2^16..2^28 (powers of 4), u32 and u64; "
                          "learned: learned-bucket vs plain sort; batched: 512 clouds in one build; "
                          "cub_sort: CUB's radix sort beside this project's on the same keys (bench-only)")
     ap.add_argument("--begin-bit", type=int, default=0, help="cub_sort workload: first key bit sorted")
@@ -259,7 +261,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": octree_config(args.n),
-        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,
+                         "cpu": host_cpu()},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "details": {"sample_points": ns,
                     "what": "the oracle (C++ restatement of the reference's shaders, pinned to them; the "
@@ -290,7 +293,26 @@ def cpu_baseline(pts_np, threads, budget_s=10.0, max_reps=8):
     what = "the same" if ns == n_all else f"the first {ns} points of the"
     return {"value": round(ns * reps / el / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{reps} full builds of {what} {n_all}-point cloud with the oracle ({threads} thread"
-                      f"{'s' if threads > 1 else ''})"}
+                      f"{'s' if threads > 1 else ''})", "cpu": host_cpu()}
+
+
+def host_cpu() -> str:
+    """The host CPU as the OS names it, and its online core count."""
+    import platform
+
+    name = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    name = line.split(":", 1)[1].strip()
+                    break
+                if key == "cpu part" and not name:  # Arm: implementer / part numbers only
+                    name = "Arm part " + line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return f"{name or platform.processor() or platform.machine()}, {os.cpu_count()} cores online"
 
 
 # --------------------------------------------------------- measurements ---
@@ -310,6 +332,31 @@ def events_ms(stream, fn, reps, before=None):
         e1.synchronize()
         total += e0.elapsed_time(e1)
     return total / reps
+
+
+def graph_ms(stream, fn, reps):
+    """Mean time per replay of fn() captured once into a CUDA graph: `reps`
+    replays between two events on `stream`."""
+    import torch
+
+    fn()  # warm-up outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        fn()
+        g.capture_end()
+    torch.cuda.synchronize()
+    for _ in range(2):
+        g.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        g.replay()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
 
 
 def sort_keys(n, kb, and_words=0):
@@ -351,11 +398,19 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
         step()
     torch.cuda.synchronize()
     ctx.device_status()
+    # Stage split: eager sorts with events between the kernels.
     ctx.set_profiling(True)
     ctx.stage_times(reset=True)
-    ms = events_ms(stream, step, steps, restore)
+    eager_ms = events_ms(stream, step, steps, restore)
     stages = ctx.stage_times(reset=True)
     ctx.set_profiling(False)
+    ctx.device_status()
+    # Headline: CUDA-graph replays (no host launch cost, dependent launches on),
+    # (restore + sort) minus restore alone, each replayed `steps` times.
+    ms = graph_ms(stream, lambda: (restore(), step()), steps) - graph_ms(stream, restore, steps)
+    restore()
+    step()
+    torch.cuda.synchronize()
     ctx.device_status()
     kk = k.cpu().numpy().view(keys_np.dtype)
     vv = v.cpu().numpy().view(np.uint32)
@@ -367,7 +422,9 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     avg = os_ms / max(os_n, 1)
     pass_bytes = 2 * (K + 4) * n
     peak, _ = measured_hbm_peak()
-    return {"mkeys_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4), "n": n, "passes": passes,
+    return {"mkeys_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4), "eager_ms": round(eager_ms, 4),
+            "timing": "CUDA-graph replay of (restore + sort) minus replay of restore; stages from eager sorts",
+            "n": n, "passes": passes,
             "pass_ms": round(avg, 5), "pass_hbm_frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
             "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4),
             "hist_ms": round(stages["histogram"][0] / max(stages["histogram"][1], 1), 4),
@@ -733,6 +790,38 @@ def run_gtc_sort(args):
     ctx.close()
 
 
+def run_gtc_sort_sweep(args):
+    """Sort-only sweep of the sort config: n = 2^16 .. 2^28 in powers of 4,
+    u32 and u64 pairs (u32 values = the input index), uniform keys; each size
+    runs the autotuner's pick for its keys.  One JSON line; its value is the
+    u64 rate at the largest size."""
+    import torch
+
+    import gtc
+
+    ctx = gtc.Context(0)
+    rows = []
+    with ClockSampler(0) as clk:
+        for kb in (32, 64):
+            for lg in range(16, 29, 2):
+                r, _ = measure_sort(ctx, kb, 1 << lg, args.steps, args.warmup, 0, args.sort_variant)
+                rows.append({"key_bits": kb, "log2n": lg, "mkeys_s": r["mkeys_s"], "ms": r["ms"],
+                             "pass_hbm_frac": r["pass_hbm_frac"], "sort_hbm_frac": r["sort_hbm_frac"],
+                             "variant": r["sort_variant"], "digit_bits": r["digit_bits"], "sorted_ok": r["sorted_ok"]})
+                torch.cuda.empty_cache()
+    top = rows[-1]
+    line = {
+        "metric": "Mkeys/s sort", "value": top["mkeys_s"], "unit": "Mkeys/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": top["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "sort_sweep_2p16_2p28_u32_u64", "n": 1 << 28, "key_bits": 64},
+        "details": {"sweep": rows, "all_sorted_ok": all(r["sorted_ok"] for r in rows)},
+        "gpu_launches": None, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def cub_library():
     """Builds (once) and loads bench-only libcubref.so: CUB's
     DeviceRadixSort::SortPairs behind a C ABI, the comparison point of the
@@ -974,6 +1063,8 @@ def main():
         run_reference(args)
     elif args.workload == "cub_sort":
         run_cub_sort(args)
+    elif args.workload == "sort_sweep":
+        run_gtc_sort_sweep(args)
     elif args.workload == "sort":
         run_gtc_sort(args)
     elif args.workload == "learned":
