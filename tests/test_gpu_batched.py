@@ -54,7 +54,8 @@ def _run_batch(ctx, oracle, pts, offsets, tag):
     return results
 
 
-def test_batched_edge_cases(ctx, oracle):
+@pytest.mark.parametrize("variant", [0, 1, 3], ids=["512x12", "256x16", "512x8"])
+def test_batched_edge_cases(ctx, oracle, variant):
     clouds = [
         np.zeros((0, 4), np.float32),                       # empty first cloud
         _p([[1.0, 2.0, 3.0]]),                              # one point
@@ -71,9 +72,17 @@ def test_batched_edge_cases(ctx, oracle):
         W.uniform_points(6145, seed=10),                    # one tile + one key
         _p([[9.0, 9.0, 9.0]]),                              # one point, last cloud
         np.zeros((0, 4), np.float32),                       # empty last cloud
+        W.uniform_points(4096, seed=11),                    # exactly one tile of the 4096-key shapes
+        W.uniform_points(4097, seed=12),
     ]
     pts, offsets = _batch(clouds)
-    _run_batch(ctx, oracle, pts, offsets, "edge")
+    import gtc
+
+    gtc.batched_set_variant(variant)  # the tile shape also decides how the clouds are cut
+    try:
+        _run_batch(ctx, oracle, pts, offsets, f"edge/v{variant}")
+    finally:
+        gtc.batched_set_variant(-1)
 
 
 @pytest.mark.parametrize("tree_method", [1, 0], ids=["window", "karras"])
