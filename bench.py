@@ -223,7 +223,9 @@ def octree_config(n):
     name = WORKLOAD if n == N_POINTS else f"octree_clustered_{n}_u64"
     return {"workload": name, "n_points": n, "key_bits": KEY_BITS, "bits_per_axis": 21,
             "payload": "u32 point index",
-            "cloud": "32-component Gaussian mixture (sigma 0.5% of the domain) + 2% uniform noise, seed = rank"}
+            "cloud": "32-component Gaussian mixture (sigma 0.5% of the domain) + 2% uniform noise, seed = rank",
+            "l2": "no flush: inputs larger than L2 (16 B points per point; a 10M build reads 160 MB of points "
+                  "and moves ~3.2 GB)"}
 
 
 # ------------------------------------------------------------ reference ---
@@ -406,8 +408,19 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     ctx.set_profiling(False)
     ctx.device_status()
     # Headline: CUDA-graph replays (no host launch cost, dependent launches on),
-    # (restore + sort) minus restore alone, each replayed `steps` times.
-    ms = graph_ms(stream, lambda: (restore(), step()), steps) - graph_ms(stream, restore, steps)
+    # (restore + sort) minus restore alone, each replayed `steps` times.  Pairs
+    # smaller than 512 MB would stay in the 129 MB L2 between iterations: both
+    # graphs then also write a 256 MB buffer first (an L2 flush), so every
+    # sort starts from DRAM.
+    pair_bytes = (kb // 8 + 4) * n
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if pair_bytes < (512 << 20) else None
+
+    def cold_restore():
+        if flush is not None:
+            flush.fill_(1)
+        restore()
+
+    ms = graph_ms(stream, lambda: (cold_restore(), step()), steps) - graph_ms(stream, cold_restore, steps)
     restore()
     step()
     torch.cuda.synchronize()
@@ -424,6 +437,8 @@ def measure_sort(ctx, kb, n, steps, warmup, and_words=0, variant=None):
     peak, _ = measured_hbm_peak()
     return {"mkeys_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4), "eager_ms": round(eager_ms, 4),
             "timing": "CUDA-graph replay of (restore + sort) minus replay of restore; stages from eager sorts",
+            "l2": ("flushed: a 256 MB write before each timed sort" if flush is not None
+                   else "no flush: the pairs are larger than L2"),
             "n": n, "passes": passes,
             "pass_ms": round(avg, 5), "pass_hbm_frac": round(pass_bytes / (avg * 1e-3) / 1e9 / peak, 4),
             "sort_hbm_frac": round((K * n + passes * pass_bytes) / (ms * 1e-3) / 1e9 / peak, 4),
@@ -777,7 +792,8 @@ def run_gtc_sort(args):
         "metric": "Mkeys/s sort", "value": r["mkeys_s"], "unit": "Mkeys/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
-        "config": {"workload": f"sort_pairs_u{kb}_n{n}_and{args.and_words}", "n": n, "key_bits": kb},
+        "config": {"workload": f"sort_pairs_u{kb}_n{n}_and{args.and_words}", "n": n, "key_bits": kb,
+                   "l2": r["l2"]},
         "details": r,
         "roofline": {"bound": "hbm", "kernel": "onesweep pass",
                      "achieved": round(2 * (K + 4) * n / (r["pass_ms"] * 1e-3) / 1e9, 1), "peak": peak,
@@ -807,14 +823,17 @@ def run_gtc_sort_sweep(args):
                 r, _ = measure_sort(ctx, kb, 1 << lg, args.steps, args.warmup, 0, args.sort_variant)
                 rows.append({"key_bits": kb, "log2n": lg, "mkeys_s": r["mkeys_s"], "ms": r["ms"],
                              "pass_hbm_frac": r["pass_hbm_frac"], "sort_hbm_frac": r["sort_hbm_frac"],
-                             "variant": r["sort_variant"], "digit_bits": r["digit_bits"], "sorted_ok": r["sorted_ok"]})
+                             "variant": r["sort_variant"], "digit_bits": r["digit_bits"], "l2": r["l2"],
+                             "sorted_ok": r["sorted_ok"]})
                 torch.cuda.empty_cache()
     top = rows[-1]
     line = {
         "metric": "Mkeys/s sort", "value": top["mkeys_s"], "unit": "Mkeys/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": top["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": "sort_sweep_2p16_2p28_u32_u64", "n": 1 << 28, "key_bits": 64},
+        "config": {"workload": "sort_sweep_2p16_2p28_u32_u64", "n": 1 << 28, "key_bits": 64,
+                   "l2": "flushed (a 256 MB write) before each timed sort where the pairs are smaller than 512 MB, "
+                         "else inputs larger than L2"},
         "details": {"sweep": rows, "all_sorted_ok": all(r["sorted_ok"] for r in rows)},
         "gpu_launches": None, "clocks": clk.summary(),
     }
@@ -915,7 +934,8 @@ def run_cub_sort(args):
         "metric": "Mkeys/s sort (CUB comparison)", "value": round(n / (cub_ms * 1e-3) / 1e6, 1), "unit": "Mkeys/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cub_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": f"u{kb}", "data": "synthetic",
-        "config": {"workload": f"cub_sort_pairs_u{kb}_n{n}_bits{args.begin_bit}_{end}", "n": n, "key_bits": kb},
+        "config": {"workload": f"cub_sort_pairs_u{kb}_n{n}_bits{args.begin_bit}_{end}", "n": n, "key_bits": kb,
+                   "l2": "inputs as given by --n (larger than L2 from 2^24 pairs)"},
         "details": {"impl": "cub::DeviceRadixSort::SortPairs (bench-only comparison)", "passes": passes,
                     "cub_ms": round(cub_ms, 4), "cub_ms_per_pass": round(cub_ms / passes, 5),
                     "gtc_ms": round(gtc_ms, 4), "gtc_pass_ms": round(os_ms / max(os_n, 1), 5),
@@ -950,7 +970,8 @@ def run_gtc_learned(args):
         "metric": "Mkeys/s learned-bucket sort", "value": r["learned_mkeys_s"], "unit": "Mkeys/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["learned_ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": f"learned_sort_u64_n{n}", "n": n, "key_bits": 64},
+        "config": {"workload": f"learned_sort_u64_n{n}", "n": n, "key_bits": 64,
+                   "l2": "no flush: inputs larger than L2 (12 B per key)"},
         "details": r,
         "roofline": {"bound": "hbm", "kernel": "learned path (model + bucket scatter + in-bucket sort)",
                      "achieved": round(lbytes / (r["learned_ms"] * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
@@ -1034,7 +1055,8 @@ def run_gtc_batched(args):
         "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"batched_{S}_clouds_u32", "n_clouds": S, "n_points": n},
+        "config": {"workload": f"batched_{S}_clouds_u32", "n_clouds": S, "n_points": n,
+                   "l2": "no flush: inputs larger than L2 (16 B points per point)"},
         "details": {"cloud_min": int(sizes.min()), "cloud_max": int(sizes.max()), "n_unique": u, "n_oct_nodes": o,
                     "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (points alone exceed 1 GB)",
                     "timing": "CUDA-graph replay of the whole batch per step",
