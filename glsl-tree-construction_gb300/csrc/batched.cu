@@ -269,13 +269,7 @@ __global__ void __launch_bounds__(THREADS) bt_onesweep_kernel(const uint32_t* __
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (key[j] >> shift) & 255u;
-    uint32_t peers = 0xffffffffu;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const uint32_t bit = (d >> b) & 1u;
-      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-      peers &= bit ? bal : ~bal;
-    }
+    const uint32_t peers = warp_peers<8>(d);
     const int leader = 31 - __clz(peers);
     uint32_t b0 = 0;
     if (lane == leader) b0 = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));

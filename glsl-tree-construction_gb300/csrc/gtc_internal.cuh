@@ -363,6 +363,30 @@ __device__ __forceinline__ float4 corner_at(uint3 q, int level, float mn, float 
 }
 
 // ----------------------------------------------------------- warp scans ---
+// Lanes of the (full) warp whose value agrees with this lane's on bits
+// [0, BITS) of d: one ballot per bit.  Each bit's ballot predicate comes
+// straight from an and/setp, and the ballot is complemented under the same
+// predicate where this lane's bit is clear, so a bit costs the vote plus
+// about three simple instructions.  Called by all 32 lanes.
+template <int BITS>
+__device__ __forceinline__ uint32_t warp_peers(uint32_t d) {
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < BITS; ++b) {
+    uint32_t m;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b32 t;\n\t"
+        "and.b32 t, %1, %2;\n\t"
+        "setp.ne.u32 p, t, 0;\n\t"
+        "vote.sync.ballot.b32 %0, p, 0xffffffff;\n\t"
+        "@!p not.b32 %0, %0;\n\t}"
+        : "=r"(m)
+        : "r"(d), "r"(1u << b));
+    peers &= m;
+  }
+  return peers;
+}
+
 __device__ __forceinline__ uint32_t warp_inclusive_sum(uint32_t v) {
   const int lane = threadIdx.x & 31;
 #pragma unroll

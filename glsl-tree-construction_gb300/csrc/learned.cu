@@ -442,13 +442,7 @@ __global__ void __launch_bounds__(THREADS) learned_pass_kernel(
 #pragma unroll
   for (int j = 0; j < KPT; ++j) {
     const uint32_t d = (bd[j] >> shift) & mask;
-    uint32_t peers = 0xffffffffu;
-#pragma unroll
-    for (int b = 0; b < 7; ++b) {
-      const uint32_t bit = (d >> b) & 1u;
-      const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-      peers &= bit ? bal : ~bal;
-    }
+    const uint32_t peers = warp_peers<7>(d);
     const int leader = 31 - __clz(peers);
     uint32_t b0 = 0;
     if (lane == leader) b0 = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));

@@ -615,13 +615,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
       const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-      uint32_t peers = 0xffffffffu;
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        const uint32_t bit = (d >> b) & 1u;
-        const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-        peers &= bit ? bal : ~bal;
-      }
+      const uint32_t peers = warp_peers<8>(d);
       const int leader = 31 - __clz(peers);
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
@@ -658,13 +652,7 @@ __global__ void __launch_bounds__(THREADS, MINB) onesweep_kernel(const K* __rest
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
       const uint32_t d = (uint32_t)(key[j] >> shift) & dmask;
-      uint32_t peers = 0xffffffffu;
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        const uint32_t bit = (d >> b) & 1u;
-        const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-        peers &= bit ? bal : ~bal;
-      }
+      const uint32_t peers = warp_peers<8>(d);
       const int leader = 31 - __clz(peers);
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(&my_hist[d], (uint32_t)__popc(peers));
@@ -747,14 +735,7 @@ struct TmaSmem {
 template <bool MATCH>
 __device__ __forceinline__ uint32_t peer_mask(uint32_t d) {
   if (MATCH) return __match_any_sync(0xffffffffu, d);
-  uint32_t peers = 0xffffffffu;
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    const uint32_t bit = (d >> b) & 1u;
-    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? bal : ~bal;
-  }
-  return peers;
+  return warp_peers<8>(d);
 }
 
 template <class K, int THREADS, int KPT, bool HV, bool MATCH>
