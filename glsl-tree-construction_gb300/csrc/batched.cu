@@ -287,9 +287,14 @@ __global__ void __launch_bounds__(THREADS) bt_onesweep_kernel(const uint32_t* __
     s.gbase[tid] = seg_base[((size_t)r.cloud * BPASSES + pass) * BRADIX + tid] + excl - doff;
   }
   __syncthreads();
+  // o stays inside the cloud while every look-back completes; after one ran
+  // out (DEV_TIMEOUT) a later pass may see digit counts that disagree with
+  // the cloud's histogram, and the check keeps its writes in bounds.
+  const uint32_t end = off[r.cloud + 1];
   for (uint32_t i = tid; i < r.valid; i += THREADS) {
     const uint32_t k = s.keys[i];
     const uint32_t o = s.gbase[(k >> shift) & 255u] + i;
+    if (o >= end) continue;
     kout[o] = k;
     vout[o] = s.vals[i];
   }

@@ -461,10 +461,14 @@ __global__ void __launch_bounds__(THREADS) learned_pass_kernel(
     s.gbase[tid] = bin_off[tid] + excl - doff;
   }
   __syncthreads();
+  // o < n while every look-back completes; after one ran out (DEV_TIMEOUT)
+  // the second pass may read ids that disagree with the bucket histogram,
+  // and the check keeps its writes in bounds.
   const uint32_t valid = min((uint32_t)TILE, n - tbase);
   for (uint32_t i = tid; i < valid; i += THREADS) {
     const uint32_t b = s.bids[i];
     const uint32_t o = s.gbase[(b >> shift) & mask] + i;
+    if (o >= n) continue;
     kout[o] = s.keys[i];
     vout[o] = s.vals[i];
     if (FIRST) bout[o] = (uint16_t)b;
