@@ -51,22 +51,23 @@ constexpr int BS_THREADS = 512;    // in-bucket sort: two CTAs per SM
 constexpr int BS_CAP = 8192;       // keys per bucket sorted on chip
 constexpr int BS_IPT = BS_CAP / BS_THREADS;
 constexpr int kFallbackVariant = 4;  // onesweep variant of the fallback: persistent, TMA-fed
-constexpr int MAX_BUCKETS = 16384;  // the Eytzinger knots + bucket histogram fill one CTA's shared memory
+constexpr int MAX_BUCKETS = 16384;  // the count kernel's knots, heights and counters fill one CTA's shared memory
 
 // ---------------------------------------------------------------- model ---
-// Per-segment bucket line, derived from the heights before every sort:
-// t(key) = a + c * float(key - kn[s]) clamped to amax, with a = B * y[s],
-// amax = B * y[s + 1], c = B * (y[s + 1] - y[s]) / float(kn[s + 1] - kn[s]).
-// Every operation is one IEEE round-to-nearest step (no contraction), so the
-// oracle (orc_pwl_buckets) evaluates the same function bit for bit.  For
+// Bucket line of segment s (knots k0 = kn[s], k1 = kn[s + 1], heights y0 =
+// y[s], y1 = y[s + 1]): t(key) = a + c * float(key - k0) clamped to amax, with
+// a = B * y0, amax = B * y1, c = B * (y1 - y0) / float(k1 - k0).  Every
+// operation is one IEEE round-to-nearest step (no contraction), so the oracle
+// (orc_pwl_buckets) evaluates the same function bit for bit.  For
 // non-decreasing heights t is non-decreasing in the key: inside a segment
 // each rounding step is monotone and c >= 0; at a knot the segment's clamp
 // amax equals the next segment's start a.  bucket = floor(t) is therefore
 // monotone, which makes bucket key ranges ordered by construction.
-__device__ __forceinline__ int model_bucket(uint64_t key, int seg, const uint64_t* kn, const float4* segp, int B) {
-  const float4 p = __ldg(segp + seg);
-  const uint64_t k0 = __ldg(kn + seg);
-  const float t = fminf(__fadd_rn(p.x, __fmul_rn(p.y, __ull2float_rn(key - k0))), p.z);
+__device__ __forceinline__ int pwl_bucket(uint64_t key, uint64_t k0, uint64_t k1, float y0, float y1, int B) {
+  const float fb = (float)B;
+  const float dy = __fmul_rn(fb, __fsub_rn(y1, y0));
+  const float c = (k1 > k0 && dy > 0.0f) ? __fdiv_rn(dy, __ull2float_rn(k1 - k0)) : 0.0f;
+  const float t = fminf(__fadd_rn(__fmul_rn(fb, y0), __fmul_rn(c, __ull2float_rn(key - k0))), __fmul_rn(fb, y1));
   return min(__float2int_rz(t), B - 1);
 }
 
@@ -217,20 +218,13 @@ constexpr int kLpNumVariants = sizeof(kLpVariants) / sizeof(kLpVariants[0]);
 constexpr int LP_MIN_TILE = 4096;  // smallest tile of any variant: sizes the descriptors
 constexpr int LP_RADIX = 128;      // bucket-id digits of at most 7 bits
 
-// 0. model preparation before a sort (one thread per segment): the bucket
-// lines of model_bucket, the interior knots in Eytzinger order for the
-// count kernel's search, and the monotonicity check of the heights.
-__global__ void learned_prepare_kernel(const uint64_t* kn, const float* y, int B, uint64_t* eytz, float4* segp,
-                                       uint32_t* flags) {
+// 0. model preparation before a sort (one thread per segment): the interior
+// knots in Eytzinger order for the count kernel's search, and the
+// monotonicity check of the heights.
+__global__ void learned_prepare_kernel(const uint64_t* kn, const float* y, int B, uint64_t* eytz, uint32_t* flags) {
   const int d = 31 - __clz(B);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B; i += gridDim.x * blockDim.x) {
-    const float y0 = y[i], y1 = y[i + 1];
-    const uint64_t k0 = kn[i], k1 = kn[i + 1];
-    const float fb = (float)B;
-    const float dy = __fmul_rn(fb, __fsub_rn(y1, y0));
-    const float c = (k1 > k0 && dy > 0.0f) ? __fdiv_rn(dy, __ull2float_rn(k1 - k0)) : 0.0f;
-    segp[i] = make_float4(__fmul_rn(fb, y0), c, __fmul_rn(fb, y1), 0.0f);
-    if (flags && !(y0 <= y1)) atomicOr(flags, LFLAG_BAD_MODEL);
+    if (flags && !(y[i] <= y[i + 1])) atomicOr(flags, LFLAG_BAD_MODEL);
     if (i > 0) {  // node i of the perfect tree over interior knots 1..B-1
       const int L = 31 - __clz(i);
       const int rank = ((2 * (i - (1 << L)) + 1) << (d - 1 - L)) - 1;  // in-order position
@@ -240,35 +234,65 @@ __global__ void learned_prepare_kernel(const uint64_t* kn, const float* y, int B
 }
 
 // 1. bucket of every key (written as u16 when bids is set) and the bucket
-// histogram.  One resident CTA per SM loops over the keys; the interior knots
-// sit in shared memory in Eytzinger (breadth-first) order, so the lanes of a
-// warp walking down the tree read neighbouring words at every level, and each
-// thread walks LC_ILP keys at once to keep several shared-memory loads in
-// flight.  The segment's bucket line then comes from global memory (L1/L2).
+// histogram.  One resident CTA per SM loops over the keys.  Everything the
+// model needs sits in shared memory: the interior knots in Eytzinger
+// (breadth-first) order, so the lanes of a warp walking down the tree read
+// neighbouring words at every level; the B + 1 heights; and the counters.
+// The knots are kept as two word arrays: a level compares the high words and
+// reads the low word only where they are equal.  The walk also names the
+// segment's end knots: in a search tree the last node where the walk turned
+// right holds the largest knot <= key (kn[seg]) and the last node where it
+// turned left the smallest knot > key (kn[seg + 1]); both are read back off
+// the leaf index.  So a key costs no global load beyond itself (the segment
+// constants from global memory were one 32-sector L1 request per warp each).
+// Each thread walks LC_ILP keys at once to keep several shared-memory loads in
+// flight.  The counters are 16-bit halves of 32-bit words (the heights take
+// the room): a counter that wraps needs more than 65,535 keys of one bucket
+// in one CTA, far above the on-chip capacity, so the CTA flags OVERFLOW (the
+// sort falls back), found from the sum of its counters; without a flag word
+// (the histogram entry point) it counts its keys again with global atomics.
+__device__ __forceinline__ uint64_t knot_at(const uint32_t* s_hi, const uint32_t* s_lo, uint32_t node) {
+  return ((uint64_t)s_hi[node] << 32) | s_lo[node];
+}
+
+// Bucket of a key whose walk ended at leaf (B <= leaf < 2B).
+__device__ __forceinline__ int leaf_bucket(uint64_t key, uint32_t leaf, const uint32_t* s_hi, const uint32_t* s_lo,
+                                           const float* s_y, uint64_t kmax, int B) {
+  const int seg = (int)leaf - B;
+  const uint32_t rn = leaf >> __ffs(leaf);   // last right turn; 0 (slot of kn[0]) when none
+  const uint32_t ln = leaf >> __ffs(~leaf);  // last left turn; 0 when none (kn[B])
+  const uint64_t k0 = knot_at(s_hi, s_lo, rn);
+  const uint64_t k1 = ln ? knot_at(s_hi, s_lo, ln) : kmax;
+  return pwl_bucket(key, k0, k1, s_y[seg], s_y[seg + 1], B);
+}
+
 __global__ void __launch_bounds__(LC_THREADS, 1) learned_count_kernel(const uint64_t* __restrict__ keys, uint32_t n,
                                                                       const uint64_t* __restrict__ eytz,
                                                                       const uint64_t* __restrict__ kn,
-                                                                      const float4* __restrict__ segp, int B,
-                                                                      uint32_t* totals, uint16_t* __restrict__ bids) {
+                                                                      const float* __restrict__ y, int B,
+                                                                      uint32_t* totals, uint16_t* __restrict__ bids,
+                                                                      uint32_t* flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // The tree's knots as two word arrays: a level compares the high words and
-  // reads the low word only where they are equal, so most levels move 4
-  // bytes per lane instead of 8 (half the shared-memory wavefronts).
   uint32_t* s_hi = reinterpret_cast<uint32_t*>(smem_raw);
   uint32_t* s_lo = s_hi + B;
-  uint32_t* s_hist = s_lo + B;
+  float* s_y = reinterpret_cast<float*>(s_lo + B);                 // [B + 1]
+  uint32_t* s_hist = reinterpret_cast<uint32_t*>(s_y + B + 1);     // [B / 2]: counters 2w, 2w + 1
   for (int i = threadIdx.x; i < B; i += LC_THREADS) {
-    const uint64_t e = (i > 0) ? eytz[i] : 0ull;
+    const uint64_t e = (i > 0) ? eytz[i] : kn[0];  // slot 0 (no tree node): the lowest knot
     s_hi[i] = (uint32_t)(e >> 32);
     s_lo[i] = (uint32_t)e;
-    s_hist[i] = 0;
+    s_y[i] = y[i];
   }
+  for (int i = threadIdx.x; i < B / 2; i += LC_THREADS) s_hist[i] = 0;
+  if (threadIdx.x == 0) s_y[B] = y[B];
+  const uint64_t kmax = kn[B];
   __syncthreads();
   const int levels = 31 - __clz(B);
   const uint32_t step = gridDim.x * LC_THREADS * LC_ILP;
+  uint32_t mine = 0;  // keys counted by this thread
   for (uint32_t base = blockIdx.x * LC_THREADS * LC_ILP + threadIdx.x; base < n; base += step) {
     uint64_t k[LC_ILP];
-    int node[LC_ILP];
+    uint32_t node[LC_ILP];
 #pragma unroll
     for (int j = 0; j < LC_ILP; ++j) {
       const uint32_t i = base + j * LC_THREADS;
@@ -287,23 +311,59 @@ __global__ void __launch_bounds__(LC_THREADS, 1) learned_count_kernel(const uint
         const uint32_t h = s_hi[node[j]];
         // knot <= key: high words decide unless equal
         const bool right = (h != kh[j]) ? (h < kh[j]) : (s_lo[node[j]] <= kl[j]);
-        node[j] = 2 * node[j] + (right ? 1 : 0);
+        node[j] = 2 * node[j] + (right ? 1u : 0u);
       }
     }
 #pragma unroll
     for (int j = 0; j < LC_ILP; ++j) {
       const uint32_t i = base + j * LC_THREADS;
       if (i < n) {
-        const int b = model_bucket(k[j], node[j] - B, kn, segp, B);
-        atomicAdd(&s_hist[b], 1u);
+        const int b = leaf_bucket(k[j], node[j], s_hi, s_lo, s_y, kmax, B);
+        atomicAdd(&s_hist[b >> 1], 1u << ((b & 1) * 16));
         if (bids) bids[i] = (uint16_t)b;
+        ++mine;
       }
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < B; b += LC_THREADS) {
-    const uint32_t c = s_hist[b];
-    if (c) atomicAdd(totals + b, c);
+  // Flush; a wrapped counter shows as a shortfall of the counters' sum.
+  uint32_t sum = 0;
+  for (int w = threadIdx.x; w < B / 2; w += LC_THREADS) {
+    const uint32_t c = s_hist[w];
+    sum += (c & 0xffffu) + (c >> 16);
+  }
+  __shared__ uint32_t s_short;  // keys counted minus the counters' sum, mod 2^32: 0 unless one wrapped
+  if (threadIdx.x == 0) s_short = 0;
+  __syncthreads();
+  const uint32_t d = __reduce_add_sync(0xffffffffu, mine - sum);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&s_short, d);
+  __syncthreads();
+  if (!s_short) {
+    for (int w = threadIdx.x; w < B / 2; w += LC_THREADS) {
+      const uint32_t c = s_hist[w];
+      if (c & 0xffffu) atomicAdd(totals + 2 * w, c & 0xffffu);
+      if (c >> 16) atomicAdd(totals + 2 * w + 1, c >> 16);
+    }
+    return;
+  }
+  if (flags) {  // the sort: some bucket holds more than 65,535 keys, far above BS_CAP
+    if (threadIdx.x == 0) atomicOr(flags, LFLAG_OVERFLOW);
+    return;
+  }
+  // The histogram entry point: count this CTA's keys again, exactly.
+  for (uint32_t base = blockIdx.x * LC_THREADS * LC_ILP + threadIdx.x; base < n; base += step) {
+    for (int j = 0; j < LC_ILP; ++j) {
+      const uint32_t i = base + j * LC_THREADS;
+      if (i >= n) continue;
+      const uint64_t key = keys[i];
+      const uint32_t kh = (uint32_t)(key >> 32), kl = (uint32_t)key;
+      uint32_t nd = 1;
+      for (int l = 0; l < levels; ++l) {
+        const uint32_t h = s_hi[nd];
+        nd = 2 * nd + (((h != kh) ? (h < kh) : (s_lo[nd] <= kl)) ? 1u : 0u);
+      }
+      atomicAdd(totals + leaf_bucket(key, nd, s_hi, s_lo, s_y, kmax, B), 1u);
+    }
   }
 }
 
@@ -818,7 +878,6 @@ struct gtc_learned_model {
   uint64_t* knots = nullptr;   // [B + 1]
   float* heights = nullptr;    // [B + 1]
   uint64_t* eytz = nullptr;    // [B]: interior knots in Eytzinger order (derived before each sort)
-  float4* segp = nullptr;      // [B]: per-segment bucket lines (derived before each sort)
   float* m1 = nullptr;         // Adam moments [B + 1]
   float* m2 = nullptr;
   float* grad = nullptr;       // [B + 1]
@@ -838,25 +897,26 @@ gtc_status cuda_fail(gtc_ctx* ctx, const char* what, cudaError_t e) {
     if (_e != cudaSuccess) return cuda_fail(ctx, #expr, _e); \
   } while (0)
 
-// Count kernel: Eytzinger knots + per-bucket counters.
-size_t count_smem_bytes(int B) { return (size_t)B * 12; }
+// Count kernel: Eytzinger knots (two word arrays of B), the B + 1 heights and
+// B 16-bit counters: 14 B + 4 bytes, 229,380 at 2^14 buckets.
+size_t count_smem_bytes(int B) { return (size_t)B * 14 + 4; }
 
 // Derives the sort-time model arrays from the knots and heights.
 gtc_status prepare_model(gtc_ctx* ctx, const gtc_learned_model* m, uint32_t* d_flags, cudaStream_t s) {
-  learned_prepare_kernel<<<ceil_div(m->B, 256), 256, 0, s>>>(m->knots, m->heights, m->B, m->eytz, m->segp, d_flags);
+  learned_prepare_kernel<<<ceil_div(m->B, 256), 256, 0, s>>>(m->knots, m->heights, m->B, m->eytz, d_flags);
   LTRY(ctx, cudaGetLastError());
   return GTC_OK;
 }
 
 // The count kernel over the keys: one resident CTA per SM.
 gtc_status launch_count(gtc_ctx* ctx, const gtc_learned_model* m, const uint64_t* keys, uint32_t n, uint32_t* totals,
-                        uint16_t* bids, cudaStream_t s) {
+                        uint16_t* bids, uint32_t* d_flags, cudaStream_t s) {
   const int B = m->B;
   LTRY(ctx, kernel_setup(learned_count_kernel, LC_THREADS, count_smem_bytes(MAX_BUCKETS)));
   const Launch L = context_launch(ctx, reinterpret_cast<gtc_stream_t>(s));
   const uint32_t grid = max(1u, min((uint32_t)L.num_sms, ceil_div(n, LC_THREADS * LC_ILP)));
-  learned_count_kernel<<<grid, LC_THREADS, count_smem_bytes(B), s>>>(keys, n, m->eytz, m->knots, m->segp, B, totals,
-                                                                     bids);
+  learned_count_kernel<<<grid, LC_THREADS, count_smem_bytes(B), s>>>(keys, n, m->eytz, m->knots, m->heights, B,
+                                                                     totals, bids, d_flags);
   LTRY(ctx, cudaGetLastError());
   return GTC_OK;
 }
@@ -928,7 +988,6 @@ GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learn
   if (e == cudaSuccess) e = cudaMalloc(&m->grad, nb * 4);
   if (e == cudaSuccess) e = cudaMalloc(&m->loss, 256);
   if (e == cudaSuccess) e = cudaMalloc(&m->eytz, (size_t)buckets * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&m->segp, (size_t)buckets * 16);
   if (e != cudaSuccess) {
     gtc_learned_model_destroy(m);
     return cuda_fail(ctx, "allocating the learned model", e);
@@ -939,7 +998,7 @@ GTC_API gtc_status gtc_learned_model_create(gtc_ctx* ctx, int buckets, gtc_learn
 
 GTC_API gtc_status gtc_learned_model_destroy(gtc_learned_model* m) {
   if (!m) return GTC_OK;
-  void* ptrs[] = {m->knots, m->heights, m->m1, m->m2, m->grad, m->loss, m->sample, m->eytz, m->segp};
+  void* ptrs[] = {m->knots, m->heights, m->m1, m->m2, m->grad, m->loss, m->sample, m->eytz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete m;
@@ -1016,7 +1075,7 @@ GTC_API gtc_status gtc_learned_histogram_u64(gtc_ctx* ctx, const gtc_learned_mod
   if (n == 0) return GTC_OK;
   gtc_status st = prepare_model(ctx, m, nullptr, s);
   if (st != GTC_OK) return st;
-  return launch_count(ctx, m, keys, n, d_counts, nullptr, s);
+  return launch_count(ctx, m, keys, n, d_counts, nullptr, nullptr, s);
 }
 
 }  // extern "C"
@@ -1060,7 +1119,7 @@ gtc_status learned_sort_variant(gtc_ctx* ctx, const gtc_learned_model* m, const 
   LTRY(ctx, cudaMemsetAsync(W.totals, 0, (size_t)B * 4, s));
   LTRY(ctx, cudaMemsetAsync(W.desc, 0, 2 * W.desc_words * 4, s));
   gtc_status st = prepare_model(ctx, m, d_flags, s);
-  if (st == GTC_OK) st = launch_count(ctx, m, keys, n, W.totals, W.bid, s);
+  if (st == GTC_OK) st = launch_count(ctx, m, keys, n, W.totals, W.bid, d_flags, s);
   if (st != GTC_OK) return st;
   learned_scan_kernel<<<1, 1024, 0, s>>>(W.totals, B, db1, m->heights, W.base, W.off1, W.off2, d_flags);
   LTRY(ctx, cudaGetLastError());

@@ -120,6 +120,26 @@ def test_duplicates_and_equal_keys(ctx, oracle, gtc_mod):
         assert (int(flags.item()) != 0) == must_fall_back
 
 
+def test_wrapped_bucket_counter(ctx, oracle, gtc_mod):
+    """The count kernel keeps 16-bit per-CTA counters.  12M copies of one
+    key put about 79K keys of one bucket into every CTA: the counter wraps.
+    The histogram entry point must still be exact (the CTA counts again) and
+    the sort must flag the overflow and come out exact through the fallback."""
+    model, _ = _trained(ctx, oracle, gtc_mod, buckets=1024)
+    base = _keys(oracle, 500_000, seed=6)
+    keys = np.concatenate([np.full(12_000_000, base[3], np.uint64), base])
+    np.random.default_rng(1).shuffle(keys)
+    kn, hy = model.params()
+    exp = np.bincount(oracle.pwl_buckets(keys, kn, hy), minlength=1024)
+    got = model.histogram(_dev(keys)).cpu().numpy()
+    assert np.array_equal(got.astype(np.int64), exp)
+    ko, vo, flags = model.sort(_dev(keys))
+    assert int(flags.item()) & 1
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(ko.cpu().numpy().view(np.uint64), keys[order])
+    assert np.array_equal(vo.cpu().numpy().view(np.uint32), order.astype(np.uint32))
+
+
 def test_training_gain_over_the_untrained_model(ctx, oracle, gtc_mod):
     """What training gains, on the learned workload's keys (64-component
     mixture, 8M keys, 2^11 buckets; the model fitted to a 1% sample of a prior
