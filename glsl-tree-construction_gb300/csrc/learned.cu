@@ -684,9 +684,32 @@ __device__ __forceinline__ int bucket_sort_body(BucketSmem& s, uint32_t cnt, int
   for (int p = 0; p < np; ++p) bucket_pass<IPT>(s, cnt, ipt, 8 * p, cur, nullptr);
   if (vbits > BS_SORT_BITS) {
     uint16_t* ix = s.idx[cur];
-    for (uint32_t i = tid; i < cnt; i += BS_THREADS) {
+    // Run starts of a contiguous chunk of ipt positions per thread, found from
+    // one batch of independent reads: w[k] is the word at position
+    // q0 + k - 1 (the chunk and both neighbours), and bit k of eq says that
+    // w[k] equals w[k - 1].  Reads that fall inside another thread's run
+    // while it is being reordered still see a word of that run: equal.
+    const uint32_t q0 = (uint32_t)tid * (uint32_t)ipt;
+    uint32_t starts = 0;
+    if (q0 < cnt) {
+      const uint32_t len = min((uint32_t)ipt, cnt - q0);
+      uint32_t w[IPT + 2];
+#pragma unroll
+      for (int k = 0; k < IPT + 2; ++k) {
+        const uint32_t p = q0 + (uint32_t)k - 1u;  // wraps past 0 for k = 0 of the first chunk
+        // sort words are below 2^24: the sentinels equal neither them nor each other
+        w[k] = ((uint32_t)k <= len + 1u && p < cnt) ? s.sk[ix[p]] : 0x1000000u + (uint32_t)k;
+      }
+      uint32_t eq = 0;
+#pragma unroll
+      for (int k = 1; k < IPT + 2; ++k) eq |= (w[k] == w[k - 1] ? 1u : 0u) << k;
+      // position q0 + j starts a run: it equals the next (bit j + 2), not the previous (bit j + 1)
+      starts = (eq >> 2) & ~(eq >> 1) & ((1u << len) - 1u);
+    }
+    while (starts) {
+      const uint32_t i = q0 + (uint32_t)(__ffs(starts) - 1);
+      starts &= starts - 1u;
       const uint32_t h = s.sk[ix[i]];
-      if (i > 0 && s.sk[ix[i - 1]] == h) continue;  // not a run start
       uint32_t e = i + 1;
       while (e < cnt && e - i <= (uint32_t)BS_RUN_LIMIT && s.sk[ix[e]] == h) ++e;
       if (e - i > (uint32_t)BS_RUN_LIMIT) {
